@@ -1,0 +1,165 @@
+/*
+ * libmobility_gb300 -- C ABI of the GB300-native NBody mobility solver.
+ *
+ * One handle is one solver object with the behaviour of libMobility's
+ * `NBody` class (solvers/NBody/mobility.h) behind the `libmobility::Mobility`
+ * interface (include/MobilityInterface/MobilityInterface.h:56-224).  Every
+ * entry point below replaces one member of that interface; the reference
+ * location is cited beside each declaration.
+ *
+ * Conventions
+ *   - Every call returns an lmg_status; 0 is success.  After a failure,
+ *     lmg_last_error(h) holds the message (the reference's exception text
+ *     where it has one, e.g. "...has fallen below the wall...").
+ *   - Real-valued buffers hold `real` values: float for a handle created with
+ *     LMG_PRECISION_FLOAT, double for LMG_PRECISION_DOUBLE (the reference's
+ *     compile-time `real`, include/MobilityInterface/defines.h:5-14, made a
+ *     run-time choice).
+ *   - A buffer is a (pointer, count) pair: the count of `real` values, as in
+ *     the reference's device_span (include/memory/container.h:24-57).  A count
+ *     of 0 (or a NULL pointer) means the array is absent.
+ *   - Pointers may be host memory or CUDA device memory of the current device;
+ *     the library finds out which (cudaPointerGetAttributes) and stages host
+ *     buffers itself, as the reference's device_adapter does
+ *     (include/memory/container.h:59-110).  The caller keeps ownership of
+ *     every buffer; the library never frees them.
+ *   - Work is issued on the handle's CUDA stream (see lmg_set_stream).  Calls
+ *     that take or return host memory, and calls that must report an error
+ *     found on the GPU (setPositions, sqrtMdotW), synchronise that stream
+ *     before returning; Mdot on device buffers does not.
+ *   - A handle is not thread-safe; distinct handles are independent.
+ */
+#ifndef LIBMOBILITY_GB300_H
+#define LIBMOBILITY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lmg_solver lmg_solver;
+
+typedef enum {
+  LMG_OK = 0,
+  LMG_ERR_INVALID_ARGUMENT = 1, /* bad periodicity, shape, batch, parameter */
+  LMG_ERR_NOT_INITIALIZED = 2,  /* initialize() has not been called */
+  LMG_ERR_NO_POSITIONS = 3,     /* setPositions() has not been called */
+  LMG_ERR_BELOW_WALL = 4,       /* a particle centre is below the wall */
+  LMG_ERR_NO_CONVERGENCE = 5,   /* Lanczos reached its iteration limit */
+  LMG_ERR_NAN = 6,              /* NaN in the Lanczos result estimate */
+  LMG_ERR_TIMEOUT = 7,          /* a device-side wait ran out */
+  LMG_ERR_CUDA = 8,             /* CUDA runtime error */
+  LMG_ERR_NO_DEVICE = 9,        /* no CUDA device visible */
+  LMG_ERR_INTERNAL = 10
+} lmg_status;
+
+typedef enum { LMG_PRECISION_FLOAT = 0, LMG_PRECISION_DOUBLE = 1 } lmg_precision;
+
+/* Lanczos progress callback: iteration index and current residual, the
+ * reference's Parameters::lanczosCallback (MobilityInterface.h:42). */
+typedef void (*lmg_lanczos_callback)(int iteration, double residual, void *user);
+
+/* Interface version string, LIBMOBILITYVERSION ("1.1"),
+ * include/MobilityInterface/defines.h:4. */
+const char *lmg_version(void);
+
+/* Message of the last failed call on h (never NULL). */
+const char *lmg_last_error(const lmg_solver *h);
+
+/* NBody(Configuration) -- solvers/NBody/mobility.h:37-47 with the periodicity
+ * strings of include/MobilityInterface/pythonify.h:38-61 ("open",
+ * "single_wall", "two_walls", "periodic", "unspecified").  X and Y must be
+ * "open"; Z "open" selects the open-boundary RPY kernel, "single_wall" the
+ * Rotne-Prager-Blake kernel.  On failure *out is NULL and the message is
+ * available from lmg_create_error(). */
+lmg_status lmg_create(const char *periodicityX, const char *periodicityY,
+                      const char *periodicityZ, int precision, lmg_solver **out);
+const char *lmg_create_error(void);
+
+/* Frees the handle and everything it owns. */
+lmg_status lmg_destroy(lmg_solver *h);
+
+/* Issue work on this CUDA stream (a cudaStream_t; NULL = the handle's own
+ * stream, created on first use). */
+lmg_status lmg_set_stream(lmg_solver *h, void *cuda_stream);
+
+/* setParametersNBody -- solvers/NBody/mobility.h:78-97 and the Python
+ * setParameters of solvers/NBody/python_wrapper.cu:50-61.  algorithm is one
+ * of "fast", "naive", "block", "advise" (all run the same GB300 kernel;
+ * anything else is an error).  Nbatch/NperBatch < 0 mean "all particles in
+ * one batch".  has_wall_height says whether wallHeight was given: required for
+ * a single wall, forbidden for open Z.  delta: random-finite-difference step
+ * in units of the radius. */
+lmg_status lmg_set_parameters_nbody(lmg_solver *h, const char *algorithm,
+                                    int Nbatch, int NperBatch,
+                                    int has_wall_height, double wallHeight,
+                                    double delta);
+
+/* Mobility::initialize + NBody::initialize -- MobilityInterface.h:102-114,
+ * mobility.h:99-114.  seed 0 draws a random seed.  callback may be NULL. */
+lmg_status lmg_initialize(lmg_solver *h, double viscosity,
+                          double hydrodynamicRadius, int includeAngular,
+                          double tolerance, uint64_t seed,
+                          lmg_lanczos_callback callback, void *user);
+
+/* NBody::setPositions -- mobility.h:116-162.  pos holds n_pos = 3N reals,
+ * [x1,y1,z1,x2,...]. */
+lmg_status lmg_set_positions(lmg_solver *h, const void *pos, size_t n_pos);
+
+/* NBody::getNumberParticles -- mobility.h:164. */
+lmg_status lmg_get_number_particles(const lmg_solver *h, int64_t *out);
+
+/* Mobility::getIncludeAngular -- MobilityInterface.h:217. */
+lmg_status lmg_get_include_angular(const lmg_solver *h, int *out);
+
+/* NBody::Mdot -- mobility.h:166-182 / NbodyRPY.cu:254-287.  U (and W when
+ * includeAngular) are OVERWRITTEN with M.[F;T]. */
+lmg_status lmg_mdot(lmg_solver *h, const void *F, size_t nF, const void *T,
+                    size_t nT, void *U, size_t nU, void *W, size_t nW);
+
+/* Mobility::sqrtMdotW -- MobilityInterface.h:132-188 with the Lanczos solver
+ * of include/lanczos/LanczosAlgorithm.cu:173-232.  ADDS prefactor*sqrt(M) dW
+ * into U (and W), dW drawn from the handle's seeded generator. */
+lmg_status lmg_sqrt_mdot_w(lmg_solver *h, void *U, size_t nU, void *W,
+                           size_t nW, double prefactor);
+
+/* Same with the Gaussian vector dW given by the caller (n_dW = 3N, or 6N with
+ * includeAngular, in the layout [dW_F; dW_T]); the reference draws dW inside
+ * (include/MobilityInterface/lanczos.h:43-58).  iterations / residual (may be
+ * NULL) receive the Lanczos iteration index at return and the last
+ * successive-iterate error. */
+lmg_status lmg_sqrt_mdot_w_noise(lmg_solver *h, const void *dW, size_t n_dW,
+                                 void *U, size_t nU, void *W, size_t nW,
+                                 double prefactor, int *iterations,
+                                 double *residual);
+
+/* Mobility::LangevinVelocities -- MobilityInterface.h:191-206:
+ * U,W = M.[F;T] (if F or T given) + sqrt(2 kbt/dt) sqrt(M) dW + kbt divM. */
+lmg_status lmg_langevin_velocities(lmg_solver *h, double dt, double kbt,
+                                   const void *F, size_t nF, const void *T,
+                                   size_t nT, void *U, size_t nU, void *W,
+                                   size_t nW);
+
+/* NBody::divM -- mobility.h:184-236 (random finite differences,
+ * include/MobilityInterface/random_finite_differences.h:30-63).  ADDS
+ * prefactor * div M into U (and W); nothing for open Z. */
+lmg_status lmg_div_m(lmg_solver *h, void *U, size_t nU, void *W, size_t nW,
+                     double prefactor);
+
+/* Mobility::clean -- MobilityInterface.h:220-223: frees the solver's
+ * Lanczos storage and scratch. */
+lmg_status lmg_clean(lmg_solver *h);
+
+/* Waits for the handle's stream. */
+lmg_status lmg_synchronize(lmg_solver *h);
+
+/* Precision of the handle: "float" or "double" (Mobility::precision,
+ * MobilityInterface.h:73-77). */
+const char *lmg_precision_name(const lmg_solver *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LIBMOBILITY_GB300_H */

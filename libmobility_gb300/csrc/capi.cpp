@@ -1,0 +1,168 @@
+// extern "C" boundary: every entry point of include/libmobility_gb300.h.
+// Exceptions never cross it; they become an lmg_status plus a message.
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "solver.hpp"
+
+struct lmg_solver {
+  std::unique_ptr<lmg::SolverBase> impl;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+template <class F> lmg_status guarded(lmg_solver *h, F &&f) {
+  if (!h || !h->impl) return LMG_ERR_INVALID_ARGUMENT;
+  try {
+    f(*h->impl);
+    h->impl->last_error.clear();
+    return LMG_OK;
+  } catch (const lmg::Error &e) {
+    h->impl->last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    h->impl->last_error = "[libmobility_gb300] out of host memory";
+    return LMG_ERR_INTERNAL;
+  } catch (const std::exception &e) {
+    h->impl->last_error = e.what();
+    return LMG_ERR_INTERNAL;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+const char *lmg_version(void) { return "1.1"; }
+
+const char *lmg_last_error(const lmg_solver *h) {
+  if (!h || !h->impl) return "invalid handle";
+  return h->impl->last_error.c_str();
+}
+
+const char *lmg_create_error(void) { return g_create_error.c_str(); }
+
+lmg_status lmg_create(const char *px, const char *py, const char *pz, int precision,
+                      lmg_solver **out) {
+  if (!out) return LMG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  try {
+    if (!px || !py || !pz) throw lmg::Error(LMG_ERR_INVALID_ARGUMENT, "[libMobility] Invalid periodicity");
+    auto x = lmg::parse_periodicity(px);
+    auto y = lmg::parse_periodicity(py);
+    auto z = lmg::parse_periodicity(pz);
+    auto *h = new lmg_solver;
+    h->impl.reset(lmg::make_solver(x, y, z, precision));
+    *out = h;
+    g_create_error.clear();
+    return LMG_OK;
+  } catch (const lmg::Error &e) {
+    g_create_error = e.what();
+    return e.code;
+  } catch (const std::exception &e) {
+    g_create_error = e.what();
+    return LMG_ERR_INTERNAL;
+  }
+}
+
+lmg_status lmg_destroy(lmg_solver *h) {
+  if (!h) return LMG_ERR_INVALID_ARGUMENT;
+  delete h;
+  return LMG_OK;
+}
+
+lmg_status lmg_set_stream(lmg_solver *h, void *s) {
+  return guarded(h, [&](lmg::SolverBase &m) { m.set_stream((cudaStream_t)s); });
+}
+
+lmg_status lmg_set_parameters_nbody(lmg_solver *h, const char *algorithm, int Nbatch,
+                                    int NperBatch, int has_wall_height, double wallHeight,
+                                    double delta) {
+  return guarded(h, [&](lmg::SolverBase &m) {
+    // string2NBodyAlgorithm, solvers/NBody/python_wrapper.cu:35-47.  All four
+    // schedules run the same GB300 kernel.
+    std::string a = algorithm ? algorithm : "advise";
+    if (a != "naive" && a != "fast" && a != "block" && a != "advise")
+      throw lmg::Error(LMG_ERR_INVALID_ARGUMENT, "Invalid algorithm selected");
+    std::optional<double> wh;
+    if (has_wall_height) wh = wallHeight;
+    m.set_parameters(Nbatch, NperBatch, wh, delta);
+  });
+}
+
+lmg_status lmg_initialize(lmg_solver *h, double viscosity, double radius, int includeAngular,
+                          double tolerance, uint64_t seed, lmg_lanczos_callback cb, void *user) {
+  return guarded(h, [&](lmg::SolverBase &m) {
+    m.initialize(viscosity, radius, includeAngular != 0, tolerance, seed, cb, user);
+  });
+}
+
+lmg_status lmg_set_positions(lmg_solver *h, const void *pos, size_t n) {
+  return guarded(h, [&](lmg::SolverBase &m) { m.set_positions(pos, pos ? n : 0); });
+}
+
+lmg_status lmg_get_number_particles(const lmg_solver *h, int64_t *out) {
+  if (!h || !h->impl || !out) return LMG_ERR_INVALID_ARGUMENT;
+  *out = h->impl->number_particles();
+  return LMG_OK;
+}
+
+lmg_status lmg_get_include_angular(const lmg_solver *h, int *out) {
+  if (!h || !h->impl || !out) return LMG_ERR_INVALID_ARGUMENT;
+  *out = h->impl->include_angular() ? 1 : 0;
+  return LMG_OK;
+}
+
+lmg_status lmg_mdot(lmg_solver *h, const void *F, size_t nF, const void *T, size_t nT, void *U,
+                    size_t nU, void *W, size_t nW) {
+  return guarded(h, [&](lmg::SolverBase &m) { m.mdot(F, nF, T, nT, U, nU, W, nW); });
+}
+
+lmg_status lmg_sqrt_mdot_w(lmg_solver *h, void *U, size_t nU, void *W, size_t nW,
+                           double prefactor) {
+  return guarded(h, [&](lmg::SolverBase &m) {
+    m.sqrt_mdot_w(U, nU, W, nW, prefactor, nullptr, 0, nullptr, nullptr);
+  });
+}
+
+lmg_status lmg_sqrt_mdot_w_noise(lmg_solver *h, const void *dW, size_t n_dW, void *U, size_t nU,
+                                 void *W, size_t nW, double prefactor, int *iterations,
+                                 double *residual) {
+  return guarded(h, [&](lmg::SolverBase &m) {
+    if (!dW || n_dW == 0)
+      throw lmg::Error(LMG_ERR_INVALID_ARGUMENT, "[libmobility_gb300] dW is required");
+    m.sqrt_mdot_w(U, nU, W, nW, prefactor, dW, n_dW, iterations, residual);
+  });
+}
+
+lmg_status lmg_langevin_velocities(lmg_solver *h, double dt, double kbt, const void *F,
+                                   size_t nF, const void *T, size_t nT, void *U, size_t nU,
+                                   void *W, size_t nW) {
+  return guarded(h, [&](lmg::SolverBase &m) { m.langevin(dt, kbt, F, nF, T, nT, U, nU, W, nW); });
+}
+
+lmg_status lmg_div_m(lmg_solver *h, void *U, size_t nU, void *W, size_t nW, double prefactor) {
+  return guarded(h, [&](lmg::SolverBase &m) { m.div_m(U, nU, W, nW, prefactor); });
+}
+
+lmg_status lmg_clean(lmg_solver *h) {
+  return guarded(h, [&](lmg::SolverBase &m) { m.clean(); });
+}
+
+lmg_status lmg_synchronize(lmg_solver *h) {
+  return guarded(h, [&](lmg::SolverBase &m) { m.synchronize(); });
+}
+
+const char *lmg_precision_name(const lmg_solver *h) {
+  if (!h || !h->impl) return "";
+  return h->impl->precision();
+}
+
+// Internal test hook (not part of the public header): FP64 T^{1/2} e1 of a
+// symmetric tridiagonal matrix with the solver's own QL routine, on the host.
+int lmg_internal_tridiag_sqrt_e1(const double *alpha, const double *beta, int m, double *out) {
+  return lmg::tridiag_sqrt_e1_host(alpha, beta, m, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,79 @@
+// Shared host-side definitions: status-carrying exception and CUDA checks.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+
+#include "libmobility_gb300.h"
+
+namespace lmg {
+
+// Every failure inside the library is an Error; the C ABI turns it into an
+// lmg_status and keeps the message for lmg_last_error.
+struct Error : std::runtime_error {
+  lmg_status code;
+  Error(lmg_status c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] inline void throw_cuda(cudaError_t e, const char *what) {
+  cudaGetLastError();  // clear a sticky-free error so the handle stays usable
+  lmg_status st = (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+                      ? LMG_ERR_NO_DEVICE : LMG_ERR_CUDA;
+  throw Error(st, std::string("[libmobility_gb300] CUDA error in ") + what + ": " +
+                      cudaGetErrorString(e));
+}
+
+#define LMG_CUDA(call)                                  \
+  do {                                                  \
+    cudaError_t lmg_e_ = (call);                        \
+    if (lmg_e_ != cudaSuccess) ::lmg::throw_cuda(lmg_e_, #call); \
+  } while (0)
+
+// Owning device allocation that only grows.
+template <class T> struct DeviceBuffer {
+  T *ptr = nullptr;
+  size_t count = 0;
+  DeviceBuffer() = default;
+  DeviceBuffer(const DeviceBuffer &) = delete;
+  DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+  ~DeviceBuffer() { release(); }
+  T *ensure(size_t n) {
+    if (n > count) {
+      release();
+      LMG_CUDA(cudaMalloc((void **)&ptr, (n ? n : 1) * sizeof(T)));
+      count = n;
+    }
+    return ptr;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    count = 0;
+  }
+};
+
+// Page-locked host staging allocation that only grows.
+template <class T> struct PinnedBuffer {
+  T *ptr = nullptr;
+  size_t count = 0;
+  PinnedBuffer() = default;
+  PinnedBuffer(const PinnedBuffer &) = delete;
+  PinnedBuffer &operator=(const PinnedBuffer &) = delete;
+  ~PinnedBuffer() { release(); }
+  T *ensure(size_t n) {
+    if (n > count) {
+      release();
+      LMG_CUDA(cudaMallocHost((void **)&ptr, (n ? n : 1) * sizeof(T)));
+      count = n;
+    }
+    return ptr;
+  }
+  void release() {
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    count = 0;
+  }
+};
+
+}  // namespace lmg

@@ -1,0 +1,379 @@
+// Device side of the Lanczos evaluation of sqrt(M) dW.
+//
+// Follows the algorithm of libMobility include/lanczos/LanczosAlgorithm.cu
+// (Ando, Chow, Saad, Skolnick 2012):
+//   v0 = z/|z|                                     setFirstBasisVector :110-118
+//   w = M v_i - beta_{i-1} v_{i-1}; alpha_i = w.v_i; w -= alpha_i v_i;
+//   beta_i = |w|, zeroed if beta_i < 1e-3 alpha_i/|z| (then v_{i+1} = e1),
+//   v_{i+1} = w/beta_i                             nextIteration :120-153
+//   y = |z| V_m T_m^{1/2} e1                       computeCurrentResultEstimation :158-167
+//   err = |y_i - y_{i-1}| / |y_{i-1}|              computeError :202-222
+// GB300 choices: the Krylov vectors stay in the solver precision, every inner
+// product and norm accumulates in FP64 and the scalars alpha, beta, |z| live in
+// device memory as FP64 (no host round trip per iteration); T_m^{1/2} e1 is
+// computed on the device in FP64 by implicit QL (below).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lmg {
+
+// ---------------------------------------------------------------------------
+// Gaussian noise: Philox4x32-10 counter-based generator (Salmon, Moraes,
+// Dror, Shaw, SC'11) + Box-Muller.  Stream = (seed1, seed2), element i.
+// ---------------------------------------------------------------------------
+struct Philox {
+  static __host__ __device__ __forceinline__ void round(uint32_t c[4], uint32_t k[2]) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    const uint32_t n0 = hi1 ^ c[1] ^ k[0];
+    const uint32_t n2 = hi0 ^ c[3] ^ k[1];
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+    k[0] += 0x9E3779B9u;
+    k[1] += 0xBB67AE85u;
+  }
+  static __host__ __device__ __forceinline__ void gen(uint32_t ctr, uint32_t s1, uint32_t s2,
+                                                      uint32_t out[4]) {
+    uint32_t c[4] = {ctr, 0x6C6D6736u /* stream tag */, 0u, 0u};
+    uint32_t k[2] = {s1, s2};
+#pragma unroll
+    for (int r = 0; r < 10; r++) round(c, k);
+    out[0] = c[0];
+    out[1] = c[1];
+    out[2] = c[2];
+    out[3] = c[3];
+  }
+};
+
+// Four N(0,1) values per counter; out[4*q + r].
+template <class R>
+__global__ void gauss_fill_kernel(R *out, size_t n, uint32_t s1, uint32_t s2) {
+  const size_t nq = (n + 3) / 4;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nq;
+       q += (size_t)gridDim.x * blockDim.x) {
+    uint32_t b[4];
+    Philox::gen((uint32_t)q, s1, s2, b);
+    R z[4];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      // u1 in (0,1], u2 in [0,1) from 32 random bits each
+      const double u1 = ((double)b[2 * h] + 1.0) * 2.3283064365386963e-10;
+      const double u2 = (double)b[2 * h + 1] * 2.3283064365386963e-10;
+      if (sizeof(R) == 4) {
+        const float rr = sqrtf(-2.0f * logf((float)u1));
+        float sn, cs;
+        sincospif(2.0f * (float)u2, &sn, &cs);
+        z[2 * h] = (R)(rr * cs);
+        z[2 * h + 1] = (R)(rr * sn);
+      } else {
+        const double rr = sqrt(-2.0 * log(u1));
+        double sn, cs;
+        sincospi(2.0 * u2, &sn, &cs);
+        z[2 * h] = (R)(rr * cs);
+        z[2 * h + 1] = (R)(rr * sn);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+      if (4 * q + r < n) out[4 * q + r] = z[r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 block reduction + "last block finishes" grid reduction
+// ---------------------------------------------------------------------------
+constexpr int kRedThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sums `v` over the block; result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+  __shared__ double red[NV][kRedThreads / 32];
+#pragma unroll
+  for (int q = 0; q < NV; q++) v[q] = warp_sum(v[q]);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) red[q][wid] = v[q];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      double x = lane < kRedThreads / 32 ? red[q][lane] : 0.0;
+      v[q] = warp_sum(x);
+    }
+  }
+}
+
+// Publishes this block's NV partial sums; returns true in thread 0 of the
+// last block to arrive, whose `tot` then holds the grid totals (summed in
+// block order, so the result does not depend on arrival order).
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double (&v)[NV], double *partials,
+                                         unsigned *ticket, double (&tot)[NV]) {
+  __shared__ bool s_last;
+  block_sum<NV>(v);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) __stcg(partials + (size_t)q * gridDim.x + blockIdx.x, v[q]);
+    __threadfence();
+    const unsigned prev = atomicAdd(ticket, 1u);
+    s_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  // the last block sums the partials cooperatively
+  double acc[NV];
+#pragma unroll
+  for (int q = 0; q < NV; q++) acc[q] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) acc[q] += __ldcg(partials + (size_t)q * gridDim.x + b);
+  }
+  block_sum<NV>(acc);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) tot[q] = acc[q];
+    *ticket = 0u;
+  }
+  return threadIdx.x == 0;
+}
+
+// Scalars of one solve, FP64, in device memory.
+struct KrylovScalars {
+  double normz;       // |z|
+  double err;         // last successive-iterate error
+  int status;         // 0 ok, 1 QL failure
+  int pad;
+  double alpha[256];  // diagonal of T
+  double beta[256];   // off-diagonal of T (beta[i] couples i and i+1)
+};
+
+// |z|^2 -> normz, and v0 = z/|z| (two kernels: the norm is a grid reduction)
+template <class R>
+__global__ void krylov_norm_kernel(const R *z, size_t n, double *partials, unsigned *ticket,
+                                   KrylovScalars *sc) {
+  double v[1] = {0.0};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double x = (double)z[e];
+    v[0] += x * x;
+  }
+  double tot[1];
+  if (grid_sum<1>(v, partials, ticket, tot)) sc->normz = sqrt(tot[0]);
+}
+
+template <class R>
+__global__ void krylov_scale_first_kernel(const R *z, R *v0, size_t n, const KrylovScalars *sc) {
+  const R inv = (R)(1.0 / sc->normz);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x)
+    v0[e] = z[e] * inv;
+}
+
+// w -= beta_{i-1} v_{i-1};  alpha_i = w . v_i
+template <class R>
+__global__ void krylov_alpha_kernel(R *w, const R *vi, const R *vprev, size_t n, int i,
+                                    double *partials, unsigned *ticket, KrylovScalars *sc) {
+  const R bprev = i > 0 ? (R)sc->beta[i - 1] : R(0);
+  double v[1] = {0.0};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    R x = w[e];
+    if (i > 0) x -= bprev * vprev[e];
+    w[e] = x;
+    v[0] += (double)x * (double)vi[e];
+  }
+  double tot[1];
+  if (grid_sum<1>(v, partials, ticket, tot)) sc->alpha[i] = tot[0];
+}
+
+// w -= alpha_i v_i;  beta_i = |w| with the breakdown rule
+template <class R>
+__global__ void krylov_beta_kernel(R *w, const R *vi, size_t n, int i, double *partials,
+                                   unsigned *ticket, KrylovScalars *sc) {
+  const R al = (R)sc->alpha[i];
+  double v[1] = {0.0};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const R x = w[e] - al * vi[e];
+    w[e] = x;
+    v[0] += (double)x * (double)x;
+  }
+  double tot[1];
+  if (grid_sum<1>(v, partials, ticket, tot)) {
+    double b = sqrt(tot[0]);
+    const double tol = 1e-3 * sc->alpha[i] / sc->normz;  // LanczosAlgorithm.cu:141-143
+    if (b < tol) b = 0.0;
+    sc->beta[i] = b;
+  }
+}
+
+// v_{i+1} = w / beta_i, or e1 after a breakdown (LanczosAlgorithm.cu:144-152)
+template <class R>
+__global__ void krylov_next_kernel(const R *w, R *vnext, size_t n, int i, const KrylovScalars *sc) {
+  const double b = sc->beta[i];
+  const R inv = b > 0.0 ? (R)(1.0 / b) : R(0);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x)
+    vnext[e] = b > 0.0 ? w[e] * inv : (e == 0 ? R(1) : R(0));
+}
+
+// ---------------------------------------------------------------------------
+// T_m^{1/2} e1 in FP64: implicit QL with Wilkinson shifts on the symmetric
+// tridiagonal T_m (the tql1/tql2 family of Bowdler, Martin, Reinsch and
+// Wilkinson, Numer. Math. 11, 1968).  Only the first row of the eigenvector
+// matrix Q is carried through the sweeps (O(1) per rotation) and every
+// rotation is logged; T^{1/2} e1 = Q diag(sqrt(lambda)) Q^T e1 is then
+// obtained by applying the logged rotations in reverse order to the vector
+// diag(sqrt(lambda)) Q^T e1.  Total work O(m^2) instead of O(m^3).
+// Negative eigenvalues give NaN, as the reference's sqrt does
+// (LanczosAlgorithm.cu:72-74), which the error test then reports.
+// ---------------------------------------------------------------------------
+struct RotLog {
+  double2 *cs;     // (c, s) per rotation
+  int *idx;        // column index i of the rotation on (i, i+1)
+  int capacity;
+};
+
+__host__ __device__ inline int tridiag_sqrt_e1(const double *alpha, const double *beta, int m,
+                                               double *d, double *e, double *q0, RotLog log,
+                                               double *out) {
+  for (int k = 0; k < m; k++) {
+    d[k] = alpha[k];
+    e[k] = k + 1 < m ? beta[k] : 0.0;
+    q0[k] = k == 0 ? 1.0 : 0.0;
+  }
+  int nrot = 0;
+  const double eps = 2.220446049250313e-16;
+  for (int l = 0; l < m; l++) {
+    int iter = 0;
+    for (;;) {
+      int mm = l;
+      for (; mm < m - 1; mm++) {
+        const double dd = fabs(d[mm]) + fabs(d[mm + 1]);
+        if (fabs(e[mm]) <= eps * dd) break;
+      }
+      if (mm == l) break;
+      if (++iter > 60) return 1;
+      // Wilkinson-type shift from the leading 2x2 block
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = hypot(g, 1.0);
+      g = d[mm] - d[l] + e[l] / (g + (g >= 0.0 ? fabs(r) : -fabs(r)));
+      double s = 1.0, c = 1.0, p = 0.0;
+      int i = mm - 1;
+      bool deflated = false;
+      for (; i >= l; i--) {
+        double f = s * e[i];
+        const double b = c * e[i];
+        r = hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {  // underflow: split the matrix here and restart
+          d[i + 1] -= p;
+          e[mm] = 0.0;
+          deflated = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - p;
+        r = (d[i] - g) * s + 2.0 * c * b;
+        p = s * r;
+        d[i + 1] = g + p;
+        g = c * r - b;
+        // rotation on columns (i, i+1):  Q <- Q G,  G = [[c, s], [-s, c]]
+        const double a0 = q0[i], a1 = q0[i + 1];
+        q0[i] = c * a0 - s * a1;
+        q0[i + 1] = s * a0 + c * a1;
+        if (nrot >= log.capacity) return 2;
+        log.cs[nrot] = make_double2(c, s);
+        log.idx[nrot] = i;
+        nrot++;
+      }
+      if (deflated) continue;
+      d[l] -= p;
+      e[l] = g;
+      e[mm] = 0.0;
+    }
+  }
+  // out = Q (sqrt(lambda) * q0), applying the logged rotations in reverse
+  for (int k = 0; k < m; k++) out[k] = sqrt(d[k]) * q0[k];
+  for (int t = nrot - 1; t >= 0; t--) {
+    const double c = log.cs[t].x, s = log.cs[t].y;
+    const int i = log.idx[t];
+    const double a0 = out[i], a1 = out[i + 1];
+    out[i] = c * a0 + s * a1;
+    out[i + 1] = -s * a0 + c * a1;
+  }
+  return 0;
+}
+
+// One thread: c = T_m^{1/2} e1 (FP64) for m = i+1.
+__global__ void krylov_tridiag_kernel(KrylovScalars *sc, int m, double *work, RotLog log,
+                                      double *c_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double *d = work, *e = work + m, *q0 = work + 2 * m;
+  const int rc = tridiag_sqrt_e1(sc->alpha, sc->beta, m, d, e, q0, log, c_out);
+  if (rc != 0) {
+    sc->status = rc;
+    for (int k = 0; k < m; k++) c_out[k] = nan("");
+  }
+}
+
+// y = |z| V_m c   (V row-major: row k is v_k, n elements)
+template <class R>
+__global__ void krylov_estimate_kernel(const R *V, size_t ldv, int m, const double *c,
+                                       const KrylovScalars *sc, R *y, size_t n) {
+  __shared__ R cs[256];
+  const double nz = sc->normz;
+  for (int k = threadIdx.x; k < m; k += blockDim.x) cs[k] = (R)(nz * c[k]);
+  __syncthreads();
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    R acc = 0;
+    for (int k = 0; k < m; k++) acc += cs[k] * V[(size_t)k * ldv + e];
+    y[e] = acc;
+  }
+}
+
+// err = |y - old| / |old| (FP64), then old = y.  first: only copy.
+template <class R>
+__global__ void krylov_error_kernel(const R *y, R *old, size_t n, int first, double *partials,
+                                    unsigned *ticket, KrylovScalars *sc) {
+  double v[2] = {0.0, 0.0};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const R yo = old[e], yn = y[e];
+    if (!first) {
+      const double a = (double)yo, dlt = (double)yn - (double)yo;
+      v[0] += a * a;
+      v[1] += dlt * dlt;
+    }
+    old[e] = yn;
+  }
+  if (first) return;
+  double tot[2];
+  if (grid_sum<2>(v, partials, ticket, tot)) sc->err = fabs(sqrt(tot[1]) / sqrt(tot[0]));
+}
+
+// out += pf * y  (used for both the linear and the angular halves)
+template <class R>
+__global__ void axpy_kernel(R *out, const R *y, size_t n, R pf) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x)
+    out[e] += pf * y[e];
+}
+
+}  // namespace lmg

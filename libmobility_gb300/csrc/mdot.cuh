@@ -1,0 +1,355 @@
+// Tiled all-pairs RPY mobility product M.[F;T] for sm_103a.
+//
+// Replaces the reference kernels computeRPYBatchedFastGPU / NaiveGPU /
+// NaiveBlockGPU and their launchers (libMobility
+// solvers/NBody/extra/NbodyRPY.cu:26-252): every pair (i, j) inside the same
+// batch contributes, the self pair included, and the outputs are overwritten.
+//
+// Layout and schedule:
+//   * a CTA owns BT = THREADS*TPT consecutive targets (TPT per thread,
+//     strided by THREADS so loads and stores coalesce) and one contiguous
+//     chunk of their batch's sources (blockIdx.y selects the chunk);
+//   * sources are staged through shared memory in tiles of THREADS, already
+//     divided by the radius a and, for the wall, clamped (h = max(z, a)/a)
+//     and damped (F, T pre-multiplied by b_j); every thread then reads the
+//     tile by broadcast;
+//   * tiles whose sources all lie in the targets' batch take an unrolled loop
+//     without bounds tests; batch edges take a per-pair test;
+//   * FP32 partial sums are folded every tile into (sum, compensation) pairs
+//     with the two-sum transformation, so the error does not grow with N;
+//   * when the source range is split over several CTAs, each writes its
+//     (sum, compensation) partials to scratch and the last CTA of a target
+//     tile to finish (counted with an atomic ticket) reduces them in order
+//     and writes the result; the ticket is reset by that CTA, so the scratch
+//     needs no clearing between launches and nothing waits on anything.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rpy_pair.cuh"
+
+namespace lmg {
+
+enum Geometry : int { kOpen = 0, kWall = 1 };
+
+template <class R> struct alignas(4 * sizeof(R)) Q4 { R x, y, z, w; };
+
+template <class R> struct MdotArgs {
+  const R *pos;  // 3N positions, wall frame (wall at z = 0), interleaved
+  const R *F;    // 3N forces or nullptr
+  const R *T;    // 3N torques or nullptr
+  R *U;          // 3N linear velocities (overwritten) or nullptr
+  R *W;          // 3N angular velocities (overwritten) or nullptr
+  const int *sys_begin;  // optional table of batch starts (nsys+1 entries)
+  int nsys;              // number of entries-1 in sys_begin, or 0
+  int N;                 // particles
+  int nper;              // equal batch size when sys_begin == nullptr
+  int chunk;             // sources per split (multiple of THREADS)
+  R inv_a;               // 1/a
+  PairConst<R> k;
+  R *part;               // scratch: [tiles][nsplit][2*NC][BT]
+  unsigned *ticket;      // scratch: [tiles]
+};
+
+// Two-sum fold of t into (S, C): S + C carries the running sum to about
+// one rounding of the final value (Knuth's TwoSum).
+template <class R> __device__ __forceinline__ void fold(R &S, R &C, R t) {
+  const R s = S + t;
+  const R bp = s - S;
+  C += (S - (s - bp)) + (t - bp);
+  S = s;
+}
+
+template <class R> __device__ __forceinline__ int system_of(const MdotArgs<R> &a, int i) {
+  if (a.sys_begin == nullptr) return i / a.nper;
+  int lo = 0, hi = a.nsys;  // sys_begin[lo] <= i < sys_begin[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(a.sys_begin + mid) <= i) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+template <class R> __device__ __forceinline__ int system_start(const MdotArgs<R> &a, int s) {
+  return a.sys_begin ? __ldg(a.sys_begin + s) : s * a.nper;
+}
+template <class R> __device__ __forceinline__ int system_end(const MdotArgs<R> &a, int s) {
+  int e = a.sys_begin ? __ldg(a.sys_begin + s + 1) : (s + 1) * a.nper;
+  return e < a.N ? e : a.N;
+}
+
+template <class R, int GEOM, bool HAS_F, bool HAS_T, bool ANG> struct PairKernel {
+  static constexpr bool UF = HAS_F;
+  static constexpr bool WF = HAS_F && ANG;
+  static constexpr bool UT = HAS_T && ANG;
+  static constexpr bool WT = HAS_T && ANG;
+
+  // Adds the contribution of source (p, f, t) to target (x, y, z).
+  static __device__ __forceinline__ void eval(const PairConst<R> &k, R xi, R yi, R zi,
+                                              const Q4<R> &p, const Q4<R> &fv,
+                                              const Q4<R> &tv, Vec3<R> &u, Vec3<R> &w) {
+    const R dx = xi - p.x;
+    const R dy = yi - p.y;
+    const R dz = zi - p.z;
+    const R r2 = dx * dx + dy * dy + dz * dz;
+    const R ir = dev_rsqrt<R>(r2);
+    R f = 0, G = 0, fw = 0, Gw = 0, c = 0;
+    rpy_coefficients<R, UF, WT, UT || WF>(k, r2, ir, f, G, fw, Gw, c);
+    if (UF) {
+      const R g = G * (dx * fv.x + dy * fv.y + dz * fv.z);
+      u.x += f * fv.x + g * dx;
+      u.y += f * fv.y + g * dy;
+      u.z += f * fv.z + g * dz;
+    }
+    if (UT) {  // c (T x d)
+      u.x += c * (tv.y * dz - tv.z * dy);
+      u.y += c * (tv.z * dx - tv.x * dz);
+      u.z += c * (tv.x * dy - tv.y * dx);
+    }
+    if (WT) {
+      const R g = Gw * (dx * tv.x + dy * tv.y + dz * tv.z);
+      w.x += fw * tv.x + g * dx;
+      w.y += fw * tv.y + g * dy;
+      w.z += fw * tv.z + g * dz;
+    }
+    if (WF) {  // c (F x d)
+      w.x += c * (fv.y * dz - fv.z * dy);
+      w.y += c * (fv.z * dx - fv.x * dz);
+      w.z += c * (fv.x * dy - fv.y * dx);
+    }
+    if (GEOM == kWall) {
+      // image vector R = (dx, dy, h_i + h_j), shared by all blocks
+      const R Rz = zi + p.z;
+      const R iR = dev_rsqrt<R>(dx * dx + dy * dy + Rz * Rz);
+      const R ex = dx * iR, ey = dy * iR, ez = Rz * iR;
+      Vec3<R> cu = {0, 0, 0}, cw = {0, 0, 0}, ct = {0, 0, 0}, cf = {0, 0, 0};
+      const Vec3<R> F3 = {fv.x, fv.y, fv.z};
+      const Vec3<R> T3 = {tv.x, tv.y, tv.z};
+      if (r2 > R(0)) {
+        const R iRz = dev_div<R>(R(1), Rz);
+        const R hj = p.z * iRz;  // h_j / R_z
+        if (UF) wall_uf_pair<R>(ex, ey, ez, iR, hj, F3, cu);
+        if (WT) wall_wt_pair<R>(ex, ey, ez, iR, T3, cw);
+        if (WF) wall_wf_pair<R>(ex, ey, ez, iR, hj, F3, cf);
+        if (UT) wall_ut_pair<R>(-ex, -ey, ez, iR, zi * iRz, T3, ct);
+      } else {
+        const R ih = dev_div<R>(R(1), p.z);
+        if (UF) wall_self_uf<R>(ih, F3, cu);
+        if (WT) wall_self_wt<R>(ih, T3, cw);
+        if (WF) wall_self_wf<R>(ih, F3, cf);
+        if (UT) wall_self_ut<R>(ih, T3, ct);
+      }
+      if (UF) { u.x += k.t0 * cu.x; u.y += k.t0 * cu.y; u.z += k.t0 * cu.z; }
+      if (UT) { u.x += k.rt0 * ct.x; u.y += k.rt0 * ct.y; u.z += k.rt0 * ct.z; }
+      if (WT) { w.x += k.r0 * cw.x; w.y += k.r0 * cw.y; w.z += k.r0 * cw.z; }
+      if (WF) { w.x += k.rt0 * cf.x; w.y += k.rt0 * cf.y; w.z += k.rt0 * cf.z; }
+    }
+  }
+};
+
+template <class R, int GEOM, bool HAS_F, bool HAS_T, bool ANG, int TPT, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+mdot_kernel(const MdotArgs<R> a) {
+  using PK = PairKernel<R, GEOM, HAS_F, HAS_T, ANG>;
+  constexpr int BT = THREADS * TPT;
+  constexpr bool USE_T = HAS_T && ANG;
+  constexpr int NC = ANG ? 6 : 3;  // accumulated components per target
+  constexpr bool COMP = sizeof(R) == 4;  // compensated accumulation in FP32
+
+  __shared__ Q4<R> sp[THREADS];
+  __shared__ Q4<R> sf[HAS_F ? THREADS : 1];
+  __shared__ Q4<R> st[USE_T ? THREADS : 1];
+  __shared__ int s_last;
+
+  const int N = a.N;
+  const int tile = blockIdx.x;
+  const int split = blockIdx.y;
+  const int nsplit = gridDim.y;
+  const int tgt0 = tile * BT;
+  const R ia = a.inv_a;
+
+  // ---- targets ----
+  R xi[TPT], yi[TPT], zi[TPT], bi[TPT];
+  int lo[TPT], hi[TPT];
+#pragma unroll
+  for (int t = 0; t < TPT; t++) {
+    int i = tgt0 + threadIdx.x + t * THREADS;
+    int ic = i < N ? i : N - 1;
+    R x = a.pos[3 * ic], y = a.pos[3 * ic + 1], z = a.pos[3 * ic + 2];
+    xi[t] = x * ia;
+    yi[t] = y * ia;
+    if (GEOM == kWall) {
+      R zs = z * ia;
+      bi[t] = zs < R(0) ? R(0) : (zs > R(1) ? R(1) : zs);
+      zi[t] = zs > R(1) ? zs : R(1);
+    } else {
+      zi[t] = z * ia;
+      bi[t] = R(1);
+    }
+    int s = system_of(a, ic);
+    lo[t] = system_start(a, s);
+    hi[t] = system_end(a, s);
+  }
+  // batch range of the whole CTA
+  const int last = (tgt0 + BT < N ? tgt0 + BT : N) - 1;
+  const int s_first = system_of(a, tgt0);
+  const int s_lastb = system_of(a, last);
+  const int src_lo = system_start(a, s_first);
+  const int src_hi = system_end(a, s_lastb);
+  const bool uniform = (s_first == s_lastb);
+  const int c_begin = src_lo + split * a.chunk;
+  const int c_end = min(src_hi, c_begin + a.chunk);
+
+  Vec3<R> u[TPT], w[TPT];
+  R S[TPT][NC], C[TPT][NC];
+#pragma unroll
+  for (int t = 0; t < TPT; t++) {
+    u[t] = {0, 0, 0};
+    w[t] = {0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < NC; c++) { S[t][c] = 0; C[t][c] = 0; }
+  }
+
+  for (int ts = c_begin; ts < c_end; ts += THREADS) {
+    {  // stage one tile of sources
+      const int j = ts + threadIdx.x;
+      Q4<R> p = {0, 0, 0, 0}, fv = {0, 0, 0, 0}, tv = {0, 0, 0, 0};
+      if (j < c_end) {
+        R x = a.pos[3 * j], y = a.pos[3 * j + 1], z = a.pos[3 * j + 2];
+        R b = R(1);
+        p.x = x * ia;
+        p.y = y * ia;
+        if (GEOM == kWall) {
+          R zs = z * ia;
+          b = zs < R(0) ? R(0) : (zs > R(1) ? R(1) : zs);
+          p.z = zs > R(1) ? zs : R(1);
+        } else {
+          p.z = z * ia;
+        }
+        if (HAS_F) { fv.x = b * a.F[3 * j]; fv.y = b * a.F[3 * j + 1]; fv.z = b * a.F[3 * j + 2]; }
+        if (USE_T) { tv.x = b * a.T[3 * j]; tv.y = b * a.T[3 * j + 1]; tv.z = b * a.T[3 * j + 2]; }
+      }
+      sp[threadIdx.x] = p;
+      if (HAS_F) sf[threadIdx.x] = fv;
+      if (USE_T) st[threadIdx.x] = tv;
+    }
+    __syncthreads();
+    const int n_here = min(THREADS, c_end - ts);
+    if (uniform && n_here == THREADS) {
+#pragma unroll 4
+      for (int jj = 0; jj < THREADS; jj++) {
+        const Q4<R> p = sp[jj];
+        const Q4<R> fv = HAS_F ? sf[jj] : Q4<R>{0, 0, 0, 0};
+        const Q4<R> tv = USE_T ? st[jj] : Q4<R>{0, 0, 0, 0};
+#pragma unroll
+        for (int t = 0; t < TPT; t++) PK::eval(a.k, xi[t], yi[t], zi[t], p, fv, tv, u[t], w[t]);
+      }
+    } else {
+      for (int jj = 0; jj < n_here; jj++) {
+        const int j = ts + jj;
+        const Q4<R> p = sp[jj];
+        const Q4<R> fv = HAS_F ? sf[jj] : Q4<R>{0, 0, 0, 0};
+        const Q4<R> tv = USE_T ? st[jj] : Q4<R>{0, 0, 0, 0};
+#pragma unroll
+        for (int t = 0; t < TPT; t++)
+          if (j >= lo[t] && j < hi[t]) PK::eval(a.k, xi[t], yi[t], zi[t], p, fv, tv, u[t], w[t]);
+      }
+    }
+    // fold the tile's partial sums
+#pragma unroll
+    for (int t = 0; t < TPT; t++) {
+      R v[6] = {u[t].x, u[t].y, u[t].z, w[t].x, w[t].y, w[t].z};
+#pragma unroll
+      for (int c = 0; c < NC; c++) {
+        if (COMP) fold(S[t][c], C[t][c], v[c]); else S[t][c] += v[c];
+      }
+      u[t] = {0, 0, 0};
+      w[t] = {0, 0, 0};
+    }
+    __syncthreads();
+  }
+
+  if (nsplit == 1) {
+#pragma unroll
+    for (int t = 0; t < TPT; t++) {
+      const int i = tgt0 + threadIdx.x + t * THREADS;
+      if (i >= N) continue;
+      if (a.U) {
+        a.U[3 * i] = bi[t] * (S[t][0] + C[t][0]);
+        a.U[3 * i + 1] = bi[t] * (S[t][1] + C[t][1]);
+        a.U[3 * i + 2] = bi[t] * (S[t][2] + C[t][2]);
+      }
+      if (ANG && a.W) {
+        a.W[3 * i] = bi[t] * (S[t][NC - 3] + C[t][NC - 3]);
+        a.W[3 * i + 1] = bi[t] * (S[t][NC - 2] + C[t][NC - 2]);
+        a.W[3 * i + 2] = bi[t] * (S[t][NC - 1] + C[t][NC - 1]);
+      }
+    }
+    return;
+  }
+
+  // ---- split sources: publish partials, last CTA of the tile reduces ----
+  R *mine = a.part + ((size_t)(tile * nsplit + split) * (2 * NC)) * BT;
+#pragma unroll
+  for (int t = 0; t < TPT; t++) {
+    const int l = threadIdx.x + t * THREADS;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+      __stcg(mine + (size_t)c * BT + l, S[t][c]);
+      __stcg(mine + (size_t)(NC + c) * BT + l, C[t][c]);
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(a.ticket + tile, 1u);
+    s_last = (prev == (unsigned)(nsplit - 1));
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const R *base = a.part + ((size_t)tile * nsplit * (2 * NC)) * BT;
+#pragma unroll
+  for (int t = 0; t < TPT; t++) {
+    const int l = threadIdx.x + t * THREADS;
+    const int i = tgt0 + l;
+    R Ss[NC], Cs[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) { Ss[c] = 0; Cs[c] = 0; }
+    for (int s = 0; s < nsplit; s++) {
+      const R *ps = base + (size_t)s * (2 * NC) * BT;
+#pragma unroll
+      for (int c = 0; c < NC; c++) {
+        const R sv = __ldcg(ps + (size_t)c * BT + l);
+        const R cv = __ldcg(ps + (size_t)(NC + c) * BT + l);
+        if (COMP) fold(Ss[c], Cs[c], sv); else Ss[c] += sv;
+        Cs[c] += cv;
+      }
+    }
+    if (i < N) {
+      if (a.U) {
+        a.U[3 * i] = bi[t] * (Ss[0] + Cs[0]);
+        a.U[3 * i + 1] = bi[t] * (Ss[1] + Cs[1]);
+        a.U[3 * i + 2] = bi[t] * (Ss[2] + Cs[2]);
+      }
+      if (ANG && a.W) {
+        a.W[3 * i] = bi[t] * (Ss[NC - 3] + Cs[NC - 3]);
+        a.W[3 * i + 1] = bi[t] * (Ss[NC - 2] + Cs[NC - 2]);
+        a.W[3 * i + 2] = bi[t] * (Ss[NC - 1] + Cs[NC - 1]);
+      }
+    }
+  }
+  if (threadIdx.x == 0) a.ticket[tile] = 0u;  // ready for the next launch
+}
+
+// Host-side launch description chosen by the planner.
+struct MdotPlan {
+  int threads = 128;
+  int tpt = 1;
+  int nsplit = 1;
+  int chunk = 0;
+  int tiles = 0;
+  size_t part_elems = 0;  // scratch elements of R needed
+  size_t tickets = 0;
+};
+
+}  // namespace lmg

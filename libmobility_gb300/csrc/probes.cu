@@ -1,0 +1,51 @@
+// Measurement hooks (not part of the public header):
+//   * a count of the kernels this library has launched, so a benchmark can
+//     state how many of its kernels ran inside a timed region;
+//   * an FP32 FMA-chain kernel whose throughput is the FP32 peak the pair
+//     kernel's roofline is quoted against (measured on the same GPU, same
+//     clocks, in the same run).
+#include <atomic>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "launch_count.hpp"
+
+namespace lmg {
+std::atomic<unsigned long long> g_launches{0};
+}
+
+namespace {
+// 8 independent FMA chains per thread, `iters` rounds of 8 FMAs each
+// (2 flops per FMA).  The result is written only if it is the impossible
+// value -1 so the compiler must keep the chains.
+__global__ void fma_chain_kernel(int iters, float *sink) {
+  float a[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) a[k] = (threadIdx.x + k) * 1e-7f;
+  const float b = 0.999999f, c = 1e-8f;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) a[k] = fmaf(a[k], b, c);
+    }
+  }
+  float s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += a[k];
+  if (s == -1.0f) sink[threadIdx.x] = s;
+}
+}  // namespace
+
+extern "C" {
+
+unsigned long long lmg_internal_launch_count(void) { return lmg::g_launches.load(); }
+
+// Launches blocks x threads of the FMA chain on `stream`; flops performed =
+// blocks * threads * iters * 64 * 2.
+int lmg_internal_fma_probe(int blocks, int threads, int iters, void *sink, void *stream) {
+  fma_chain_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, (float *)sink);
+  return (int)cudaGetLastError();
+}
+}

@@ -1,0 +1,238 @@
+// Pair physics of the NBody Rotne-Prager-Yamakawa mobility, open boundary and
+// single bottom wall, written for the tiled all-pairs kernels.
+//
+// Physics follows libMobility solvers/NBody/extra/hydrodynamicKernels.cuh:
+//   RPY_UF :41-57, RPY_WT :63-86, RPY_UT/RPY_WF :89-118 (open-space blocks),
+//   wallCorrection_UF :187-249, _WT :253-282, _UT :287-319, _WF :324-359,
+//   BottomWall::dotProduct :362-441 (damping b_i b_j, heights clamped at a,
+//   image vector r_ij + 2 h_j z, UT evaluated with -r_ij + 2 h_i z).
+//
+// Representation chosen here (not the reference's entry-by-entry matrices):
+//   * all lengths are divided by the hydrodynamic radius a when a source or a
+//     target is loaded, so r~ = r/a appears directly;
+//   * each 3x3 block is applied in vector form, e.g. the translational wall
+//     image tensor C2 is  A I + B e e^T + C e z^T + D z e^T + E z z^T,
+//     so   C2.v = A v + B (e.v) e + C v_z e + D (e.v) z + E v_z z;
+//   * the antisymmetric couplings are cross products, M_UT T = c (T x d),
+//     the wall image C3 of WF is f1 (e x F) + (f3 (e.F) + f2 F_z)(e x z)
+//     + f4 (z x F), and UT uses its transpose;
+//   * the image vector R = (dx, dy, h_i + h_j) is shared by all four blocks
+//     (UT uses (-dx, -dy, h_i + h_j)), so one rsqrt serves every block;
+//   * the damping b_i b_j and the block prefactors t0, r0, rt0 are applied
+//     outside the pair loop (sources are pre-multiplied by b_j, targets by
+//     b_i, prefactors folded into per-launch constants).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace lmg {
+
+template <class R> struct Vec3 { R x, y, z; };
+
+template <class R> __device__ __forceinline__ R dev_rsqrt(R x);
+template <> __device__ __forceinline__ float dev_rsqrt<float>(float x) { return rsqrtf(x); }
+template <> __device__ __forceinline__ double dev_rsqrt<double>(double x) { return rsqrt(x); }
+
+template <class R> __device__ __forceinline__ R dev_div(R a, R b);
+template <> __device__ __forceinline__ float dev_div<float>(float a, float b) { return __fdividef(a, b); }
+template <> __device__ __forceinline__ double dev_div<double>(double a, double b) { return a / b; }
+
+// Per-launch constants, prefactors already folded in.
+template <class R> struct PairConst {
+  // translational RPY, far:  f = ir*(tf0 + tf1*ir2), G = ir3*(tg0 + tg1*ir2)
+  R tf0, tf1, tg0, tg1;
+  // translational RPY, near: f = t0 - tn1*r, G = tn2*ir
+  R t0, tn1, tn2;
+  // rotational RPY, far: f = rf1*ir3, G = rg1*ir5
+  R rf1, rg1;
+  // rotational RPY, near: f = r0 + rn1*r + rn3*r^3, G = rn2*ir + rn4*r
+  R r0, rn1, rn3, rn2, rn4;
+  // coupling: far c = rt0*ir3, near c = rt0*(1/2 - 3/16 r)
+  R rt0, cn0, cn1;
+};
+
+template <class R>
+inline PairConst<R> make_pair_const(double t0, double r0, double rt0) {
+  PairConst<R> c;
+  c.tf0 = R(0.75 * t0);
+  c.tf1 = R(0.5 * t0);
+  c.tg0 = R(0.75 * t0);
+  c.tg1 = R(-1.5 * t0);
+  c.t0 = R(t0);
+  c.tn1 = R(0.28125 * t0);  // 9/32
+  c.tn2 = R(0.09375 * t0);  // 3/32
+  c.rf1 = R(-0.5 * r0);
+  c.rg1 = R(1.5 * r0);
+  c.r0 = R(r0);
+  c.rn1 = R(-0.84375 * r0);  // 27/32
+  c.rn3 = R(0.078125 * r0);  // 5/64
+  c.rn2 = R(0.28125 * r0);   // 9/32
+  c.rn4 = R(-0.046875 * r0); // 3/64
+  c.rt0 = R(rt0);
+  c.cn0 = R(0.5 * rt0);
+  c.cn1 = R(-0.1875 * rt0);  // 1/2 * 3/8
+  return c;
+}
+
+// Open-space RPY scalar coefficients for a pair at scaled distance r (r2 =
+// r^2, ir = 1/r).  U_UF = f F + G (d.F) d ; W_WT = fw T + Gw (d.T) d ;
+// coupling c:  U_UT = c (T x d), W_WF = c (F x d).  Self pair (r2 == 0):
+// f = t0, fw = r0, G = Gw = c = 0 (d = 0 makes the coupling vanish anyway).
+template <class R, bool TT, bool ROT, bool CPL>
+__device__ __forceinline__ void rpy_coefficients(const PairConst<R> &k, R r2, R ir,
+                                                 R &f, R &G, R &fw, R &Gw, R &c) {
+  const R ir2 = ir * ir;
+  const R ir3 = ir * ir2;
+  if (TT) {
+    f = ir * (k.tf0 + k.tf1 * ir2);
+    G = ir3 * (k.tg0 + k.tg1 * ir2);
+  }
+  if (ROT) {
+    fw = k.rf1 * ir3;
+    Gw = k.rg1 * ir3 * ir2;
+  }
+  if (CPL) c = k.rt0 * ir3;
+  if (r2 < R(4)) {  // overlapping pair (r < 2a), rare except the self pair
+    const bool self = !(r2 > R(0));
+    const R r = self ? R(0) : r2 * ir;
+    const R irs = self ? R(0) : ir;
+    if (TT) {
+      f = k.t0 - k.tn1 * r;
+      G = k.tn2 * irs;
+    }
+    if (ROT) {
+      fw = k.r0 + r * (k.rn1 + k.rn3 * r * r);
+      Gw = k.rn2 * irs + k.rn4 * r;
+      if (self) Gw = R(0);
+    }
+    if (CPL) c = k.cn0 + k.cn1 * r;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Bottom wall image corrections (Swan & Brady 2007), scaled units.
+// R = (Rx, Ry, Rz) image vector, iR = 1/|R|, hh = h/Rz (h_j for UF/WT/WF,
+// h_i for UT).  All results are *added* into the outputs.
+// ---------------------------------------------------------------------------
+
+// C2: translational image, wallCorrection_UF :203-247
+template <class R>
+__device__ __forceinline__ void wall_uf_pair(R ex, R ey, R ez, R iR, R hh,
+                                             const Vec3<R> &v, Vec3<R> &out) {
+  const R iR2 = iR * iR;
+  const R iR3 = iR2 * iR;
+  const R iR5 = iR3 * iR2;
+  const R ez2 = ez * ez;
+  const R h1 = hh * (R(1) - hh);
+  // A = -(3(1 + 2 h(1-h) ez2)/R + 2(1-3ez2)/R^3 - 2(1-5ez2)/R^5)/4
+  const R A = R(-0.25) * (R(3) * (R(1) + R(2) * h1 * ez2) * iR +
+                          R(2) * (R(1) - R(3) * ez2) * iR3 -
+                          R(2) * (R(1) - R(5) * ez2) * iR5);
+  // B = -(3(1 - 6 h(1-h) ez2)/R - 6(1-5ez2)/R^3 + 10(1-7ez2)/R^5)/4
+  const R B = R(-0.25) * (R(3) * (R(1) - R(6) * h1 * ez2) * iR -
+                          R(6) * (R(1) - R(5) * ez2) * iR3 +
+                          R(10) * (R(1) - R(7) * ez2) * iR5);
+  // C = ez (3h(1 - 6(1-h) ez2)/R - 6(1-5ez2)/R^3 + 10(2-7ez2)/R^5)/2
+  const R C = R(0.5) * ez * (R(3) * hh * (R(1) - R(6) * (R(1) - hh) * ez2) * iR -
+                             R(6) * (R(1) - R(5) * ez2) * iR3 +
+                             R(10) * (R(2) - R(7) * ez2) * iR5);
+  // D = ez (3h/R - 10/R^5)/2
+  const R D = R(0.5) * ez * (R(3) * hh * iR - R(10) * iR5);
+  // E = -(3 h^2 ez2/R + 3 ez2/R^3 + (2 - 15 ez2)/R^5)
+  const R E = -(R(3) * hh * hh * ez2 * iR + R(3) * ez2 * iR3 + (R(2) - R(15) * ez2) * iR5);
+  const R ev = ex * v.x + ey * v.y + ez * v.z;
+  const R s = B * ev + C * v.z;  // coefficient of e
+  out.x += A * v.x + s * ex;
+  out.y += A * v.y + s * ey;
+  out.z += A * v.z + s * ez + D * ev + E * v.z;
+}
+
+// C4: rotational image, wallCorrection_WT :262-280
+template <class R>
+__device__ __forceinline__ void wall_wt_pair(R ex, R ey, R ez, R iR,
+                                             const Vec3<R> &v, Vec3<R> &out) {
+  const R iR3 = iR * iR * iR;
+  const R f1 = R(0.5) * (R(1) - R(6) * ez * ez) * iR3;
+  const R f2 = R(-1.5) * iR3;
+  const R f3 = R(3) * iR3 * ez;
+  const R f4 = R(3) * iR3;
+  const R ev = ex * v.x + ey * v.y + ez * v.z;
+  const R pv = ex * v.y - ey * v.x;  // (z x e).v with z x e = (-ey, ex, 0)
+  const R s = f2 * ev;
+  out.x += f1 * v.x + s * ex - f4 * pv * ey;
+  out.y += f1 * v.y + s * ey + f4 * pv * ex;
+  out.z += f1 * v.z + s * ez + f3 * ev;
+}
+
+// C3 factors shared by WF (h = h_j) and UT (h = h_i), :296-307 / :333-345
+template <class R>
+__device__ __forceinline__ void wall_c3_factors(R ez, R iR, R hh, R &f1, R &f2,
+                                                R &f3, R &f4) {
+  const R iR2 = iR * iR;
+  const R iR4 = iR2 * iR2;
+  const R ez2 = ez * ez;
+  f1 = iR2;
+  f2 = R(2) * (R(6) * hh * ez2 * iR2 + (R(1) - R(10) * ez2) * iR4);
+  f3 = R(-2) * ez * (R(3) * hh * iR2 - R(5) * iR4);
+  f4 = R(-2) * ez * (hh * iR2 - iR4);
+}
+
+// C3 F:  f1 (e x F) + (f3 (e.F) + f2 F_z)(e x z) + f4 (z x F),  :347-356
+template <class R>
+__device__ __forceinline__ void wall_wf_pair(R ex, R ey, R ez, R iR, R hh,
+                                             const Vec3<R> &v, Vec3<R> &out) {
+  R f1, f2, f3, f4;
+  wall_c3_factors(ez, iR, hh, f1, f2, f3, f4);
+  const R ev = ex * v.x + ey * v.y + ez * v.z;
+  const R g = f3 * ev + f2 * v.z;  // times e x z = (ey, -ex, 0)
+  out.x += f1 * (ey * v.z - ez * v.y) + g * ey - f4 * v.y;
+  out.y += f1 * (ez * v.x - ex * v.z) - g * ex + f4 * v.x;
+  out.z += f1 * (ex * v.y - ey * v.x);
+}
+
+// C3^T T:  f1 (T x e) + ((e x z).T)(f3 e + f2 z) + f4 (T x z),  :309-316
+// (e here is the unit vector of the UT image (-dx, -dy, h_i + h_j)).
+template <class R>
+__device__ __forceinline__ void wall_ut_pair(R ex, R ey, R ez, R iR, R hh,
+                                             const Vec3<R> &v, Vec3<R> &out) {
+  R f1, f2, f3, f4;
+  wall_c3_factors(ez, iR, hh, f1, f2, f3, f4);
+  const R q = ey * v.x - ex * v.y;  // (e x z).T
+  out.x += f1 * (v.y * ez - v.z * ey) + q * f3 * ex + f4 * v.y;
+  out.y += f1 * (v.z * ex - v.x * ez) + q * f3 * ey - f4 * v.x;
+  out.z += f1 * (v.x * ey - v.y * ex) + q * (f3 * ez + f2);
+}
+
+// Self terms B1, B2, B3 (r == 0), :190-202, :256-261, :290-294, :327-331.
+// ih = 1/h (scaled).  Adds the UF, WT, UT, WF self corrections.
+template <class R>
+__device__ __forceinline__ void wall_self_uf(R ih, const Vec3<R> &v, Vec3<R> &out) {
+  const R ih3 = ih * ih * ih;
+  const R ih5 = ih3 * ih * ih;
+  const R cxy = R(-0.0625) * (R(9) * ih - R(2) * ih3 + ih5);
+  const R cz = R(-0.125) * (R(9) * ih - R(4) * ih3 + ih5);
+  out.x += cxy * v.x;
+  out.y += cxy * v.y;
+  out.z += cz * v.z;
+}
+template <class R>
+__device__ __forceinline__ void wall_self_wt(R ih, const Vec3<R> &v, Vec3<R> &out) {
+  const R ih3 = ih * ih * ih;
+  out.x += R(-0.3125) * ih3 * v.x;
+  out.y += R(-0.3125) * ih3 * v.y;
+  out.z += R(-0.125) * ih3 * v.z;
+}
+// WF self: (h^-4/8) (z x F);  UT self: -(h^-4/8) (z x T)
+template <class R>
+__device__ __forceinline__ void wall_self_wf(R ih, const Vec3<R> &v, Vec3<R> &out) {
+  const R c = R(0.125) * (ih * ih) * (ih * ih);
+  out.x -= c * v.y;
+  out.y += c * v.x;
+}
+template <class R>
+__device__ __forceinline__ void wall_self_ut(R ih, const Vec3<R> &v, Vec3<R> &out) {
+  const R c = R(0.125) * (ih * ih) * (ih * ih);
+  out.x += c * v.y;
+  out.y -= c * v.x;
+}
+
+}  // namespace lmg

@@ -1,0 +1,579 @@
+// Numeric half of the solver, templated on the precision `real`.
+//
+//   setPositions   solvers/NBody/mobility.h:116-162
+//   Mdot           mobility.h:166-182 -> NbodyRPY.cu:254-287
+//   sqrtMdotW      MobilityInterface.h:132-188 + lanczos.h:43-58 +
+//                  LanczosAlgorithm.cu:173-232
+//   divM           mobility.h:184-236 + random_finite_differences.h:30-63
+//   clean          MobilityInterface.h:220-223
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <vector>
+
+#include "krylov.cuh"
+#include "launch_count.hpp"
+#include "mdot_launch.cuh"
+#include "solver.hpp"
+
+namespace lmg {
+
+namespace {
+
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+template <class R>
+__global__ void shift_min_kernel(R *pos, int N, R height, double *partials, unsigned *ticket,
+                                 double *out_min) {
+  double v = 1e300;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    R z = pos[3 * i + 2];
+    if (height != R(0)) {
+      z = z - height;
+      pos[3 * i + 2] = z;
+    }
+    v = fmin(v, (double)z);
+  }
+  // min reduction through the shared grid machinery: negate and take max as sum? use block min
+  __shared__ double red[kRedThreads / 32];
+  __shared__ bool last;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = red[0];
+    for (int w = 1; w < (int)(blockDim.x / 32); w++) m = fmin(m, red[w]);
+    __stcg(partials + blockIdx.x, m);
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double m = 1e300;
+    for (int b = 0; b < (int)gridDim.x; b++) m = fmin(m, __ldcg(partials + b));
+    *out_min = m;
+    *ticket = 0u;
+  }
+}
+
+// pos_delta = pos + s * noise  (random finite differences)
+template <class R>
+__global__ void displace_kernel(const R *pos, const R *noise, R *out, size_t n, R s) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x)
+    out[e] = pos[e] + s * noise[e];
+}
+
+// out += c * (a - b)
+template <class R>
+__global__ void add_scaled_diff_kernel(R *out, const R *a, const R *b, size_t n, R c) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x)
+    out[e] += c * (a[e] - b[e]);
+}
+
+}  // namespace
+
+template <class R> class Solver final : public SolverBase {
+ public:
+  Solver(Periodicity x, Periodicity y, Periodicity z) : SolverBase(x, y, z) {}
+  ~Solver() override { release_all(); }
+
+  const char *precision() const override { return sizeof(R) == 4 ? "float" : "double"; }
+
+  void set_positions(const void *pos, size_t n) override;
+  void mdot(const void *F, size_t nF, const void *T, size_t nT, void *U, size_t nU, void *W,
+            size_t nW) override;
+  void sqrt_mdot_w(void *U, size_t nU, void *W, size_t nW, double prefactor, const void *dW,
+                   size_t ndW, int *iterations, double *residual) override;
+  void div_m(void *U, size_t nU, void *W, size_t nW, double prefactor) override;
+  void clean() override;
+
+ private:
+  // device state
+  DeviceBuffer<R> pos_, pos_tmp_;
+  DeviceBuffer<R> in_stage_, out_stage_;  // host<->device staging of user arrays
+  PinnedBuffer<R> pin_;                   // pinned bounce buffer
+  DeviceBuffer<R> part_;                  // Mdot split partials
+  DeviceBuffer<unsigned> tickets_;        // Mdot split tickets (self-resetting)
+  DeviceBuffer<double> red_part_;         // reduction partials
+  DeviceBuffer<unsigned> red_ticket_;     // reduction ticket (self-resetting)
+  DeviceBuffer<double> dmin_;
+  // Lanczos
+  DeviceBuffer<R> V_, w_, y_, old_, z_;
+  DeviceBuffer<KrylovScalars> sc_;
+  DeviceBuffer<double> cvec_, qlwork_;
+  DeviceBuffer<double2> rot_cs_;
+  DeviceBuffer<int> rot_idx_;
+  PinnedBuffer<KrylovScalars> h_sc_;
+  PinnedBuffer<double> h_dbl_;
+  // RFD
+  DeviceBuffer<R> rfd_noise_, rfd_pos_, rfd_mp_, rfd_mm_;
+  int num_sms_ = 0;
+  bool tickets_zeroed_ = false;
+  std::map<long, MdotPlan> plans_;
+
+  void release_all();
+  int sms();
+  int vec_blocks(size_t n) {
+    size_t b = (n + kRedThreads - 1) / kRedThreads;
+    size_t cap = (size_t)sms() * 4;
+    return (int)std::max<size_t>(1, std::min(b, cap));
+  }
+  void ensure_reduction(int blocks);
+  const R *device_input(const void *p, size_t n, R *stage);
+  // M . [F;T] on device buffers: the Lanczos matvec and the RFD probes
+  void mdot_device(const R *pos, const R *F, const R *T, R *U, R *W);
+  int lanczos(const R *z, R *y, size_t n, double tol, double *residual);
+};
+
+template <class R> int Solver<R>::sms() {
+  if (!num_sms_) {
+    int dev = 0;
+    LMG_CUDA(cudaGetDevice(&dev));
+    LMG_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return num_sms_;
+}
+
+template <class R> void Solver<R>::release_all() {
+  pos_.release(); pos_tmp_.release(); in_stage_.release(); out_stage_.release(); pin_.release();
+  part_.release(); tickets_.release(); red_part_.release(); red_ticket_.release(); dmin_.release();
+  V_.release(); w_.release(); y_.release(); old_.release(); z_.release(); sc_.release();
+  cvec_.release(); qlwork_.release(); rot_cs_.release(); rot_idx_.release(); h_sc_.release();
+  h_dbl_.release(); rfd_noise_.release(); rfd_pos_.release(); rfd_mp_.release(); rfd_mm_.release();
+  plans_.clear();
+  tickets_zeroed_ = false;
+}
+
+template <class R> void Solver<R>::ensure_reduction(int blocks) {
+  red_part_.ensure((size_t)4 * std::max(blocks, 1024));
+  if (!red_ticket_.ptr) {
+    red_ticket_.ensure(4);
+    LMG_CUDA(cudaMemsetAsync(red_ticket_.ptr, 0, 4 * sizeof(unsigned), stream()));
+  }
+}
+
+template <class R> void Solver<R>::set_positions(const void *pos, size_t n) {
+  if (n % 3 != 0)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libMobility] The input arrays for positions, forces, and torques must each "
+                "have total size 3*N.");
+  const int64_t N = (int64_t)(n / 3);
+  if (N > (int64_t)(1 << 30))
+    throw Error(LMG_ERR_INVALID_ARGUMENT, "[libmobility_gb300] too many particles");
+  const int64_t nb = nbatch_ < 0 ? 1 : nbatch_;
+  const int64_t np = nper_ < 0 ? N : nper_;
+  if (nb * np != N)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[Mobility] Invalid batch parameters for NBody. If in doubt, use the defaults.");
+  const char *below =
+      "[Mobility] The center of a particle has fallen below the wall. Check your "
+      "configuration and forces to ensure particle centers stay above the wall.";
+  if (N == 0) {
+    N_ = 0;
+    return;
+  }
+  const bool dev = is_device_ptr(pos);
+  if (!dev) {
+    // host input: shift and check on the host (no GPU needed to reject it)
+    const R *p = static_cast<const R *>(pos);
+    std::vector<R> tmp(p, p + n);
+    if (wall_) {
+      R zmin = std::numeric_limits<R>::max();
+      for (int64_t i = 0; i < N; i++) {
+        if (wall_height_ != 0) tmp[3 * i + 2] = tmp[3 * i + 2] - (R)wall_height_;
+        zmin = std::min(zmin, tmp[3 * i + 2]);
+      }
+      if (zmin < 0) throw Error(LMG_ERR_BELOW_WALL, below);
+    }
+    R *d = pos_tmp_.ensure(n);
+    R *h = pin_.ensure(n);
+    std::memcpy(h, tmp.data(), n * sizeof(R));
+    LMG_CUDA(cudaMemcpyAsync(d, h, n * sizeof(R), cudaMemcpyHostToDevice, stream()));
+    LMG_CUDA(cudaStreamSynchronize(stream()));
+  } else {
+    R *d = pos_tmp_.ensure(n);
+    LMG_CUDA(cudaMemcpyAsync(d, pos, n * sizeof(R), cudaMemcpyDeviceToDevice, stream()));
+    if (wall_) {
+      const int blocks = std::min<int>((int)((N + kRedThreads - 1) / kRedThreads), sms() * 4);
+      ensure_reduction(blocks);
+      dmin_.ensure(1);
+      shift_min_kernel<R><<<blocks, kRedThreads, 0, stream()>>>(
+          d, (int)N, (R)wall_height_, red_part_.ptr, red_ticket_.ptr + 3, dmin_.ptr);
+      count_launch();
+      LMG_CUDA(cudaGetLastError());
+      double *hm = h_dbl_.ensure(1);
+      LMG_CUDA(cudaMemcpyAsync(hm, dmin_.ptr, sizeof(double), cudaMemcpyDeviceToHost, stream()));
+      LMG_CUDA(cudaStreamSynchronize(stream()));
+      if (*hm < 0) throw Error(LMG_ERR_BELOW_WALL, below);
+    }
+  }
+  std::swap(pos_.ptr, pos_tmp_.ptr);
+  std::swap(pos_.count, pos_tmp_.count);
+  N_ = N;
+}
+
+// Device pointer for a user array: used in place when it is device memory,
+// otherwise copied through the pinned bounce buffer into `stage`.
+template <class R> const R *Solver<R>::device_input(const void *p, size_t n, R *stage) {
+  if (!p || n == 0) return nullptr;
+  if (is_device_ptr(p)) return static_cast<const R *>(p);
+  R *h = pin_.ensure(n);
+  std::memcpy(h, p, n * sizeof(R));
+  LMG_CUDA(cudaMemcpyAsync(stage, h, n * sizeof(R), cudaMemcpyHostToDevice, stream()));
+  // the bounce buffer is reused by the next staging: wait for this copy
+  LMG_CUDA(cudaStreamSynchronize(stream()));
+  return stage;
+}
+
+template <class R>
+void Solver<R>::mdot_device(const R *pos, const R *F, const R *T, R *U, R *W) {
+  MdotShape s;
+  s.geom = wall_ ? kWall : kOpen;
+  s.ang = ang_;
+  s.has_f = F != nullptr;
+  s.has_t = T != nullptr && ang_;
+  const int N = (int)N_;
+  const int nper = batch_size();
+  if (!s.has_f && !s.has_t) {
+    if (U) LMG_CUDA(cudaMemsetAsync(U, 0, 3 * (size_t)N * sizeof(R), stream()));
+    if (W) LMG_CUDA(cudaMemsetAsync(W, 0, 3 * (size_t)N * sizeof(R), stream()));
+    return;
+  }
+  const long key = ((long)N << 8) | (s.geom << 3) | (s.has_f << 2) | (s.has_t << 1) | s.ang;
+  auto it = plans_.find(key);
+  if (it == plans_.end() || it->second.tiles == 0) {
+    MdotPlan plan;
+    // span depends on the tile width, which the plan picks: plan twice
+    LMG_CUDA(mdot_plan<R>(s, N, N, sms(), 0, 0, plan));
+    const int span = mdot_max_span(N, nper, nullptr, 0, plan.threads * plan.tpt);
+    LMG_CUDA(mdot_plan<R>(s, N, span, sms(), plan.tpt, 0, plan));
+    it = plans_.insert_or_assign(key, plan).first;
+  }
+  const MdotPlan &plan = it->second;
+  if (plan.nsplit > 1) {
+    part_.ensure(plan.part_elems);
+    if (tickets_.count < plan.tickets || !tickets_zeroed_) {
+      tickets_.ensure(std::max(plan.tickets, tickets_.count));
+      LMG_CUDA(cudaMemsetAsync(tickets_.ptr, 0, tickets_.count * sizeof(unsigned), stream()));
+      tickets_zeroed_ = true;
+    }
+  }
+  MdotArgs<R> a{};
+  a.pos = pos;
+  a.F = F;
+  a.T = s.has_t ? T : nullptr;
+  a.U = U;
+  a.W = ang_ ? W : nullptr;
+  a.sys_begin = nullptr;
+  a.nsys = 0;
+  a.N = N;
+  a.nper = nper;
+  a.inv_a = (R)(1.0 / a_);
+  a.k = make_pair_const<R>(t0_, r0_, rt0_);
+  a.part = part_.ptr;
+  a.ticket = tickets_.ptr;
+  LMG_CUDA(mdot_launch<R>(s, a, plan, stream()));
+}
+
+template <class R>
+void Solver<R>::mdot(const void *F, size_t nF, const void *T, size_t nT, void *U, size_t nU,
+                     void *W, size_t nW) {
+  if (!F) nF = 0;
+  if (!T) nT = 0;
+  if (!U) nU = 0;
+  if (!W) nW = 0;
+  check_mdot_args(nF, nT, nU, nW);
+  const size_t n3 = 3 * (size_t)N_;
+  R *stage = in_stage_.ensure(2 * n3);
+  out_stage_.ensure(2 * n3);
+  pin_.ensure(2 * n3);
+  const R *Fd = device_input(F, nF, stage);
+  const R *Td = device_input(T, nT, stage + n3);
+  const bool u_dev = nU && is_device_ptr(U);
+  const bool w_dev = nW && is_device_ptr(W);
+  R *Ud = nU ? (u_dev ? static_cast<R *>(U) : out_stage_.ensure(2 * n3)) : nullptr;
+  R *Wd = nW ? (w_dev ? static_cast<R *>(W) : out_stage_.ensure(2 * n3) + n3) : nullptr;
+  mdot_device(pos_.ptr, Fd, Td, Ud, Wd);
+  LMG_CUDA(cudaGetLastError());
+  if ((nU && !u_dev) || (nW && !w_dev)) {
+    R *h = pin_.ensure(2 * n3);
+    if (nU && !u_dev)
+      LMG_CUDA(cudaMemcpyAsync(h, Ud, n3 * sizeof(R), cudaMemcpyDeviceToHost, stream()));
+    if (nW && !w_dev)
+      LMG_CUDA(cudaMemcpyAsync(h + n3, Wd, n3 * sizeof(R), cudaMemcpyDeviceToHost, stream()));
+    LMG_CUDA(cudaStreamSynchronize(stream()));
+    if (nU && !u_dev) std::memcpy(U, h, n3 * sizeof(R));
+    if (nW && !w_dev) std::memcpy(W, h + n3, n3 * sizeof(R));
+  }
+}
+
+// Lanczos to tolerance; returns the iteration index at convergence.
+template <class R>
+int Solver<R>::lanczos(const R *z, R *y, size_t n, double tol, double *residual) {
+  const int limit = hard_limit_;
+  const int blocks = vec_blocks(n);
+  ensure_reduction(blocks);
+  R *V = V_.ensure((size_t)(limit + 1) * n);
+  R *w = w_.ensure(n);
+  R *old = old_.ensure(n);
+  KrylovScalars *sc = sc_.ensure(1);
+  double *c = cvec_.ensure(256);
+  double *work = qlwork_.ensure(3 * 256);
+  const int rot_cap = 64 * limit * limit;
+  RotLog log{rot_cs_.ensure(rot_cap), rot_idx_.ensure(rot_cap), rot_cap};
+  KrylovScalars *hsc = h_sc_.ensure(1);
+  cudaStream_t st = stream();
+  unsigned *tk = red_ticket_.ptr;
+  double *rp = red_part_.ptr;
+  LMG_CUDA(cudaMemsetAsync(sc, 0, sizeof(KrylovScalars), st));
+  krylov_norm_kernel<R><<<blocks, kRedThreads, 0, st>>>(z, n, rp, tk, sc);
+  count_launch();
+  krylov_scale_first_kernel<R><<<blocks, kRedThreads, 0, st>>>(z, V, n, sc);
+  count_launch();
+  LMG_CUDA(cudaGetLastError());
+  const size_t n3 = 3 * (size_t)N_;
+  const int k = std::min(check_steps_, limit - 2);
+  for (int i = 0; i < limit; i++) {
+    R *vi = V + (size_t)i * n;
+    // w = M v_i  ([F;T] halves of the Krylov vector)
+    mdot_device(pos_.ptr, vi, ang_ ? vi + n3 : nullptr, w, ang_ ? w + n3 : nullptr);
+    krylov_alpha_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vi, i > 0 ? vi - n : vi, n, i, rp,
+                                                           tk, sc);
+    count_launch();
+    krylov_beta_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vi, n, i, rp, tk, sc);
+    count_launch();
+    krylov_next_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vi + n, n, i, sc);
+    count_launch();
+    if (i >= k || cb_ != nullptr) {
+      const int m = i + 1;
+      krylov_tridiag_kernel<<<1, 32, 0, st>>>(sc, m, work, log, c);
+      count_launch();
+      krylov_estimate_kernel<R><<<blocks, kRedThreads, 0, st>>>(V, n, m, c, sc, y, n);
+      count_launch();
+      krylov_error_kernel<R><<<blocks, kRedThreads, 0, st>>>(y, old, n, i == 0 ? 1 : 0, rp, tk,
+                                                             sc);
+      count_launch();
+      LMG_CUDA(cudaGetLastError());
+      if (i > 0) {
+        LMG_CUDA(cudaMemcpyAsync(hsc, sc, 2 * sizeof(double) + 2 * sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+        LMG_CUDA(cudaStreamSynchronize(st));
+        const double err = hsc->err;
+        if (residual) *residual = err;
+        if (std::isnan(err) || hsc->status != 0)
+          throw Error(LMG_ERR_NAN, "[Lanczos] Unknown error (found NaN in result guess)");
+        if (cb_) cb_(i, err, cb_user_);
+        if (err <= tol) {
+          lanczos_register(i);
+          return i;
+        }
+      }
+    }
+  }
+  LMG_CUDA(cudaStreamSynchronize(st));
+  throw Error(LMG_ERR_NO_CONVERGENCE, "[Lanczos] Could not converge");
+}
+
+template <class R>
+void Solver<R>::sqrt_mdot_w(void *U, size_t nU, void *W, size_t nW, double prefactor,
+                            const void *dW, size_t ndW, int *iterations, double *residual) {
+  if (prefactor == 0) return;
+  if (!initialized_)
+    throw Error(LMG_ERR_NOT_INITIALIZED,
+                "[libMobility] You must initialize the base class in order to use the default "
+                "stochastic displacement computation");
+  if (N_ <= 0)
+    throw Error(LMG_ERR_NO_POSITIONS,
+                "[libMobility] The number of particles is not set. Did you forget to call "
+                "setPositions?");
+  if (!U) nU = 0;
+  if (!W) nW = 0;
+  if (nU == 0)
+    throw Error(LMG_ERR_INVALID_ARGUMENT, "[libMobility] This solver requires linear velocities");
+  if (nU / 3 != (size_t)N_)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libMobility] The number of linear velocities does not match the number of "
+                "particles");
+  const size_t n3 = 3 * (size_t)N_;
+  if (nW && nW != n3)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libMobility] The number of angular velocities does not match the number of "
+                "particles");
+  const size_t n = ang_ ? 2 * n3 : n3;
+  if (dW && ndW != n)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] dW must hold 3N values (6N with includeAngular)");
+  ensure_lanczos();
+  R *z = z_.ensure(n);
+  pin_.ensure(2 * n3);
+  out_stage_.ensure(2 * n3);
+  if (dW) {
+    if (is_device_ptr(dW)) {
+      LMG_CUDA(cudaMemcpyAsync(z, dW, n * sizeof(R), cudaMemcpyDeviceToDevice, stream()));
+    } else {
+      R *h = pin_.ensure(n);
+      std::memcpy(h, dW, n * sizeof(R));
+      LMG_CUDA(cudaMemcpyAsync(z, h, n * sizeof(R), cudaMemcpyHostToDevice, stream()));
+    }
+  } else {
+    uint32_t s1, s2;
+    draw_noise_seeds(s1, s2);
+    gauss_fill_kernel<R><<<vec_blocks(n / 4 + 1), kRedThreads, 0, stream()>>>(z, n, s1, s2);
+    count_launch();
+    LMG_CUDA(cudaGetLastError());
+  }
+  R *y = y_.ensure(n);
+  double res = 0;
+  const int it = lanczos(z, y, n, tol_, &res);
+  if (iterations) *iterations = it;
+  if (residual) *residual = res;
+  // out += prefactor * y   (MobilityInterface.h:179-187)
+  const bool u_dev = is_device_ptr(U);
+  const bool w_dev = nW && is_device_ptr(W);
+  R *Ud = u_dev ? static_cast<R *>(U) : out_stage_.ensure(2 * n3);
+  R *Wd = nW ? (w_dev ? static_cast<R *>(W) : out_stage_.ensure(2 * n3) + n3) : nullptr;
+  R *h = nullptr;
+  if (!u_dev || (nW && !w_dev)) {
+    h = pin_.ensure(2 * n3);
+    if (!u_dev) std::memcpy(h, U, n3 * sizeof(R));
+    if (nW && !w_dev) std::memcpy(h + n3, W, n3 * sizeof(R));
+    if (!u_dev) LMG_CUDA(cudaMemcpyAsync(Ud, h, n3 * sizeof(R), cudaMemcpyHostToDevice, stream()));
+    if (nW && !w_dev)
+      LMG_CUDA(cudaMemcpyAsync(Wd, h + n3, n3 * sizeof(R), cudaMemcpyHostToDevice, stream()));
+  }
+  const int vb = vec_blocks(n3);
+  axpy_kernel<R><<<vb, kRedThreads, 0, stream()>>>(Ud, y, n3, (R)prefactor);
+  count_launch();
+  if (ang_ && nW) {
+    axpy_kernel<R><<<vb, kRedThreads, 0, stream()>>>(Wd, y + n3, n3, (R)prefactor);
+    count_launch();
+  }
+  LMG_CUDA(cudaGetLastError());
+  if (h) {
+    if (!u_dev) LMG_CUDA(cudaMemcpyAsync(h, Ud, n3 * sizeof(R), cudaMemcpyDeviceToHost, stream()));
+    if (nW && !w_dev)
+      LMG_CUDA(cudaMemcpyAsync(h + n3, Wd, n3 * sizeof(R), cudaMemcpyDeviceToHost, stream()));
+    LMG_CUDA(cudaStreamSynchronize(stream()));
+    if (!u_dev) std::memcpy(U, h, n3 * sizeof(R));
+    if (nW && !w_dev) std::memcpy(W, h + n3, n3 * sizeof(R));
+  } else {
+    LMG_CUDA(cudaStreamSynchronize(stream()));
+  }
+}
+
+// Thermal drift by random finite differences.  Positions are displaced in the
+// wall frame in which they are stored, so the solver's positions are left
+// exactly as they were.
+template <class R>
+void Solver<R>::div_m(void *U, size_t nU, void *W, size_t nW, double prefactor) {
+  if (prefactor == 0) return;
+  if (!wall_) return;  // no wall, no thermal drift (mobility.h:189-190)
+  if (!U) nU = 0;
+  if (!W) nW = 0;
+  const size_t n3 = 3 * (size_t)N_;
+  if (nU != n3)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libMobility] The number of forces does not match the number of particles");
+  if (ang_ && nW != n3)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libMobility] The number of torques does not match the number of particles");
+  if (!ang_ && nW != 0)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libMobility] Received torques but the solver was initialized with "
+                "includeAngular=False");
+  check_positions_set("divM");
+  const uint32_t seed = nbody_rng_();
+  R *noise = rfd_noise_.ensure(n3);
+  R *pd = rfd_pos_.ensure(n3);
+  R *mp = rfd_mp_.ensure(2 * n3);
+  R *mm = rfd_mm_.ensure(2 * n3);
+  pin_.ensure(2 * n3);
+  out_stage_.ensure(2 * n3);
+  cudaStream_t st = stream();
+  const int vb = vec_blocks(n3);
+  gauss_fill_kernel<R><<<vec_blocks(n3 / 4 + 1), kRedThreads, 0, st>>>(noise, n3, seed,
+                                                                       0x52464431u);
+  count_launch();
+  const R delta = (R)(delta_ * a_);
+  displace_kernel<R><<<vb, kRedThreads, 0, st>>>(pos_.ptr, noise, pd, n3, delta * R(0.5));
+  count_launch();
+  mdot_device(pd, noise, nullptr, mp, ang_ ? mp + n3 : nullptr);
+  displace_kernel<R><<<vb, kRedThreads, 0, st>>>(pos_.ptr, noise, pd, n3, -delta * R(0.5));
+  count_launch();
+  mdot_device(pd, noise, nullptr, mm, ang_ ? mm + n3 : nullptr);
+  LMG_CUDA(cudaGetLastError());
+  const R c = (R)(prefactor / (delta_ * a_));
+  const bool u_dev = is_device_ptr(U);
+  const bool w_dev = nW && is_device_ptr(W);
+  R *Ud = u_dev ? static_cast<R *>(U) : out_stage_.ensure(2 * n3);
+  R *Wd = nW ? (w_dev ? static_cast<R *>(W) : out_stage_.ensure(2 * n3) + n3) : nullptr;
+  R *h = nullptr;
+  if (!u_dev || (nW && !w_dev)) {
+    h = pin_.ensure(2 * n3);
+    if (!u_dev) std::memcpy(h, U, n3 * sizeof(R));
+    if (nW && !w_dev) std::memcpy(h + n3, W, n3 * sizeof(R));
+    if (!u_dev) LMG_CUDA(cudaMemcpyAsync(Ud, h, n3 * sizeof(R), cudaMemcpyHostToDevice, st));
+    if (nW && !w_dev)
+      LMG_CUDA(cudaMemcpyAsync(Wd, h + n3, n3 * sizeof(R), cudaMemcpyHostToDevice, st));
+  }
+  add_scaled_diff_kernel<R><<<vb, kRedThreads, 0, st>>>(Ud, mp, mm, n3, c);
+  count_launch();
+  if (ang_ && nW) {
+    add_scaled_diff_kernel<R><<<vb, kRedThreads, 0, st>>>(Wd, mp + n3, mm + n3, n3, c);
+    count_launch();
+  }
+  LMG_CUDA(cudaGetLastError());
+  if (h) {
+    if (!u_dev) LMG_CUDA(cudaMemcpyAsync(h, Ud, n3 * sizeof(R), cudaMemcpyDeviceToHost, st));
+    if (nW && !w_dev)
+      LMG_CUDA(cudaMemcpyAsync(h + n3, Wd, n3 * sizeof(R), cudaMemcpyDeviceToHost, st));
+    LMG_CUDA(cudaStreamSynchronize(st));
+    if (!u_dev) std::memcpy(U, h, n3 * sizeof(R));
+    if (nW && !w_dev) std::memcpy(W, h + n3, n3 * sizeof(R));
+  }
+}
+
+template <class R> void Solver<R>::clean() {
+  // Mobility::clean drops the Lanczos object (its engine and check schedule)
+  // and its storage; positions and parameters stay.
+  if (stream_) cudaStreamSynchronize(stream_);
+  lanczos_alive_ = false;
+  check_steps_ = 3;
+  V_.release(); w_.release(); y_.release(); old_.release(); z_.release();
+  rot_cs_.release(); rot_idx_.release();
+  part_.release(); tickets_.release(); tickets_zeroed_ = false; plans_.clear();
+  rfd_noise_.release(); rfd_pos_.release(); rfd_mp_.release(); rfd_mm_.release();
+}
+
+SolverBase *make_solver(Periodicity x, Periodicity y, Periodicity z, int precision) {
+  if (precision == LMG_PRECISION_DOUBLE) return new Solver<double>(x, y, z);
+  if (precision == LMG_PRECISION_FLOAT) return new Solver<float>(x, y, z);
+  throw Error(LMG_ERR_INVALID_ARGUMENT, "[libmobility_gb300] precision must be 0 (float) or 1 (double)");
+}
+
+int tridiag_sqrt_e1_host(const double *alpha, const double *beta, int m, double *out) {
+  if (m < 1 || m > 256) return 3;
+  std::vector<double> d(m), e(m), q(m);
+  const int cap = 64 * m * m + 64;
+  std::vector<double2> cs(cap);
+  std::vector<int> idx(cap);
+  RotLog log{cs.data(), idx.data(), cap};
+  return tridiag_sqrt_e1(alpha, beta, m, d.data(), e.data(), q.data(), log, out);
+}
+
+}  // namespace lmg

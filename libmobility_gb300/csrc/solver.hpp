@@ -1,0 +1,101 @@
+// Host C++ mirror of libMobility's Mobility interface and NBody solver.
+//
+//   libmobility::Mobility      include/MobilityInterface/MobilityInterface.h:56-224
+//   NBody                      solvers/NBody/mobility.h:11-237
+//
+// The non-numeric behaviour (parameter rules, error messages, seeding chain,
+// argument validation) lives in SolverBase and is identical for both
+// precisions; the numeric work is in Solver<R> (solver.cu).  Validation that
+// needs no GPU runs before any CUDA call, so it also works on a machine
+// without one.
+#pragma once
+#include <cstdint>
+#include <optional>
+#include <random>
+#include <string>
+
+#include "common.hpp"
+
+namespace lmg {
+
+enum class Periodicity { single_wall, two_walls, open, periodic, unspecified };
+
+Periodicity parse_periodicity(const std::string &s);  // pythonify.h:38-52
+
+class SolverBase {
+ public:
+  explicit SolverBase(Periodicity x, Periodicity y, Periodicity z);
+  virtual ~SolverBase();
+
+  // NBody::setParametersNBody, mobility.h:78-97 (algorithm already parsed)
+  void set_parameters(int nbatch, int nper, std::optional<double> wall_height, double delta);
+  // NBody::initialize + Mobility::initialize, mobility.h:99-114,
+  // MobilityInterface.h:102-114
+  void initialize(double viscosity, double radius, bool include_angular, double tolerance,
+                  uint64_t seed, lmg_lanczos_callback cb, void *user);
+
+  virtual void set_positions(const void *pos, size_t n) = 0;
+  virtual void mdot(const void *F, size_t nF, const void *T, size_t nT, void *U, size_t nU,
+                    void *W, size_t nW) = 0;
+  virtual void sqrt_mdot_w(void *U, size_t nU, void *W, size_t nW, double prefactor,
+                           const void *dW, size_t ndW, int *iterations, double *residual) = 0;
+  virtual void div_m(void *U, size_t nU, void *W, size_t nW, double prefactor) = 0;
+  virtual void clean() = 0;
+  virtual const char *precision() const = 0;
+
+  // Mobility::LangevinVelocities, MobilityInterface.h:191-206
+  void langevin(double dt, double kbt, const void *F, size_t nF, const void *T, size_t nT,
+                void *U, size_t nU, void *W, size_t nW);
+
+  int64_t number_particles() const { return N_; }
+  bool include_angular() const { return ang_; }
+  void set_stream(cudaStream_t s);
+  cudaStream_t stream();
+  void synchronize();
+
+  std::string last_error;
+
+ protected:
+  bool wall_ = false;
+  // setParametersNBody
+  int nbatch_ = -1, nper_ = -1;
+  double wall_height_ = 0.0;
+  double delta_ = 1e-3;
+  // initialize
+  bool initialized_ = false;
+  double a_ = 1.0, t0_ = 0, r0_ = 0, rt0_ = 0, tol_ = 1e-4;
+  bool ang_ = false;
+  std::mt19937 nbody_rng_;   // NBody::rng, draws the divM seeds
+  std::mt19937 base_rng_;    // Mobility::rng
+  uint32_t lanczos_seed_ = 0;
+  // LanczosStochasticVelocities state (lanczos.h:26-59), recreated after clean()
+  bool lanczos_alive_ = false;
+  std::mt19937 lanczos_engine_;
+  int check_steps_ = 3;      // lanczos::Solver::check_convergence_steps
+  int hard_limit_ = 200;     // lanczos::Solver::iterationHardLimit
+  lmg_lanczos_callback cb_ = nullptr;
+  void *cb_user_ = nullptr;
+  // positions
+  int64_t N_ = 0;
+  int batch_count() const { return nbatch_ < 0 ? 1 : nbatch_; }
+  int batch_size() const { return nper_ < 0 ? (int)N_ : nper_; }
+  // stream
+  cudaStream_t stream_ = nullptr;
+  bool own_stream_ = false;
+  bool user_stream_ = false;
+
+  // shared argument checks (messages of pythonify.h / mobility.h)
+  void check_positions_set(const char *who) const;
+  void check_mdot_args(size_t nF, size_t nT, size_t nU, size_t nW) const;
+  void lanczos_register(int steps);  // LanczosAlgorithm.cu:224-232
+  void ensure_lanczos();
+  void draw_noise_seeds(uint32_t &s1, uint32_t &s2);
+};
+
+SolverBase *make_solver(Periodicity x, Periodicity y, Periodicity z, int precision);
+
+// internal test hook: T^{1/2} e1 for a symmetric tridiagonal matrix (FP64,
+// host build of the device solver).  Returns 0 on success.
+int tridiag_sqrt_e1_host(const double *alpha, const double *beta, int m, double *out);
+
+}  // namespace lmg

@@ -1,0 +1,196 @@
+"""The C-ABI library on a machine without a GPU: it loads, exports every entry
+point the public header declares, and its host-side rules (periodicity,
+parameters, batches, the wall check, error messages) work before any CUDA
+call.  The FP64 tridiagonal square root used by Lanczos is checked on the host
+build of the same routine."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "libmobility_gb300.h"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from libmobility_gb300 import _build
+    _build.build()
+    from libmobility_gb300 import _capi
+    return _capi.load()
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(lmg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_symbols_exported(lib):
+    from libmobility_gb300 import _capi
+    names = declared_functions()
+    assert len(names) >= 18
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _capi.SIGNATURES, n
+    assert lib.lmg_version().decode() == "1.1"
+
+
+def _solver(pz="open", precision="float"):
+    from libmobility_gb300 import NBody
+    return NBody("open", "open", pz, precision=precision)
+
+
+def test_periodicity_rules(lib):
+    from libmobility_gb300 import NBody
+    for bad in (("periodicasdas", "periodic", "open"), ("periodic", "periodic", "open"),
+                ("open", "open", "periodic"), ("open", "open", "two_walls")):
+        with pytest.raises(RuntimeError):
+            NBody(*bad)
+    NBody("open", "open", "open")
+    NBody("open", "open", "single_wall")
+
+
+def test_wall_height_parameter_rules(lib):
+    s = _solver("open")
+    with pytest.raises(RuntimeError, match="only valid for bottom wall"):
+        s.setParameters(wallHeight=0.5)
+    s.setParameters("advise")
+    w = _solver("single_wall")
+    with pytest.raises(RuntimeError, match="required for a bottom wall"):
+        w.setParameters("advise")
+    w.setParameters(wallHeight=0.5)
+    with pytest.raises(RuntimeError, match="Invalid algorithm"):
+        s.setParameters("fmm")
+    for alg in ("naive", "fast", "block", "advise"):
+        s.setParameters(alg)
+
+
+@pytest.mark.parametrize(("nbatch", "nper", "n"), [(5, 1, 10), (2, -1, 8)])
+def test_bad_batch_parameters(lib, nbatch, nper, n):
+    s = _solver()
+    s.setParameters("advise", nbatch, nper)
+    s.initialize(viscosity=1.0, hydrodynamicRadius=1.5)
+    with pytest.raises(RuntimeError, match="Invalid batch parameters"):
+        s.setPositions(np.random.rand(n, 3))
+
+
+def test_below_wall_rejected_on_host(lib):
+    s = _solver("single_wall")
+    s.setParameters(wallHeight=1.0)
+    s.initialize(viscosity=1.0, hydrodynamicRadius=1.0)
+    with pytest.raises(RuntimeError, match="fallen below the wall"):
+        s.setPositions(np.array([1.0, 2.0, 0.5]))
+
+
+@pytest.mark.parametrize("shape", [(4, 6), (3, 1), (1, 4)])
+def test_bad_positions_shape(lib, shape):
+    s = _solver()
+    s.setParameters()
+    s.initialize(viscosity=1.0, hydrodynamicRadius=1.0)
+    with pytest.raises(RuntimeError):
+        s.setPositions(np.random.rand(*shape))
+
+
+def test_calls_before_positions(lib):
+    s = _solver()
+    s.setParameters()
+    s.initialize(viscosity=1.0, hydrodynamicRadius=1.0)
+    with pytest.raises(RuntimeError):
+        s.Mdot(np.random.rand(1, 3))
+    with pytest.raises(RuntimeError):
+        s.sqrtMdotW()
+    with pytest.raises(RuntimeError):
+        s.LangevinVelocities(dt=1.0, kbt=1.0)
+    with pytest.raises(RuntimeError):
+        s.divM()
+
+
+def test_precision_switch(lib):
+    assert _solver(precision="float").precision == "float"
+    assert _solver(precision="double").precision == "double"
+    from libmobility_gb300 import NBody
+    assert NBody.precision in ("float", "double")
+    h = _solver(precision="double")
+    assert lib.lmg_precision_name(h._h).decode() == "double"
+
+
+def test_status_codes_and_messages(lib):
+    h = ctypes.c_void_p()
+    st = lib.lmg_create(b"open", b"open", b"bogus", 0, ctypes.byref(h))
+    assert st == 1 and not h.value
+    assert b"Invalid periodicity" in lib.lmg_create_error()
+    st = lib.lmg_create(b"open", b"open", b"open", 7, ctypes.byref(h))
+    assert st == 1
+    st = lib.lmg_create(b"open", b"open", b"open", 0, ctypes.byref(h))
+    assert st == 0 and h.value
+    n = ctypes.c_int64(-1)
+    assert lib.lmg_get_number_particles(h, ctypes.byref(n)) == 0 and n.value == 0
+    # a NULL handle is rejected, not dereferenced
+    assert lib.lmg_mdot(None, None, 0, None, 0, None, 0, None, 0) == 1
+    assert lib.lmg_destroy(h) == 0
+
+
+def _tridiag_sqrt_reference(a, b):
+    from scipy.linalg import eigh_tridiagonal
+    if len(a) == 1:
+        return np.array([np.sqrt(a[0])])
+    lam, Q = eigh_tridiagonal(a, b)
+    return Q @ (np.sqrt(lam) * Q[0])
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 7, 50, 120, 200])
+def test_tridiagonal_sqrt_e1(lib, m):
+    rng = np.random.default_rng(m)
+    a = rng.uniform(1.0, 3.0, m)
+    b = rng.uniform(-0.4, 0.4, max(m - 1, 1))[: m - 1] if m > 1 else np.zeros(0)
+    # diagonally dominant -> positive definite
+    out = np.zeros(m)
+    rc = lib.lmg_internal_tridiag_sqrt_e1(a.ctypes.data, (b if m > 1 else np.zeros(1)).ctypes.data,
+                                          m, out.ctypes.data)
+    assert rc == 0
+    ref = _tridiag_sqrt_reference(a, b)
+    assert np.allclose(out, ref, rtol=1e-12, atol=1e-13)
+
+
+def test_tridiagonal_lanczos_like_spectrum(lib):
+    """Clustered and widely spread eigenvalues, as Lanczos produces (ghost
+    copies of converged eigenvalues)."""
+    rng = np.random.default_rng(3)
+    m = 60
+    lam = np.concatenate([np.full(20, 2.0) + 1e-12 * rng.normal(size=20),
+                          np.logspace(-3, 3, 40)])
+    Q, _ = np.linalg.qr(rng.normal(size=(m, m)))
+    A = Q @ np.diag(lam) @ Q.T
+    # Householder tridiagonalisation via Lanczos on A with full reorthogonalisation
+    v = rng.normal(size=m)
+    v /= np.linalg.norm(v)
+    V = [v]
+    al, be = [], []
+    w = A @ v
+    for k in range(m):
+        al.append(V[-1] @ w)
+        w = w - al[-1] * V[-1] - (be[-1] * V[-2] if k else 0)
+        for u in V:
+            w -= (u @ w) * u
+        if k == m - 1:
+            break
+        be.append(np.linalg.norm(w))
+        V.append(w / be[-1])
+        w = A @ V[-1]
+    a = np.array(al)
+    b = np.array(be)
+    out = np.zeros(m)
+    assert lib.lmg_internal_tridiag_sqrt_e1(a.ctypes.data, b.ctypes.data, m, out.ctypes.data) == 0
+    ref = _tridiag_sqrt_reference(a, b)
+    assert np.allclose(out, ref, rtol=1e-9, atol=1e-11)
+
+
+def test_tridiagonal_negative_eigenvalue_gives_nan(lib):
+    a = np.array([1.0, -2.0, 1.0])
+    b = np.array([0.1, 0.1])
+    out = np.zeros(3)
+    lib.lmg_internal_tridiag_sqrt_e1(a.ctypes.data, b.ctypes.data, 3, out.ctypes.data)
+    assert np.isnan(out).any()

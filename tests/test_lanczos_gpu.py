@@ -1,0 +1,146 @@
+"""sqrtMdotW parity on the GPU, through the C ABI.
+
+* with a given dW, against the reference lanczos::Solver fixtures and the
+  oracle's restatement: the result agrees within the Lanczos tolerance scale
+  and the iteration count matches (FP64 kernel path) or is within one;
+* fluctuation-dissipation: M^{-1/2} sqrtMdotW() samples are N(0,1) per
+  component (Kolmogorov-Smirnov, test_fluctuation_dissipation.py:19-59);
+* seeded noise: the same seed gives the same noise, the prefactor scales it;
+* the error paths (non-convergence) report an error and keep the context.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from test_mdot_gpu import compute_M, make_solver
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("precision", ["double", "float"])
+def test_against_reference_lanczos_fixture(cuda, oracle, precision):
+    z = np.load(GOLDEN / "ref_lanczos_cases.npz")
+    metas = json.loads(str(z["meta"]))
+    for si, s in enumerate(metas):
+        pos = z[f"s{si}_pos"]
+        for run in s["runs"]:
+            if run["dtype"] != "float64" or run["tol"] < 1e-6:
+                continue
+            solver = make_solver(s["wall"], s["ang"], s["a"], s["eta"], precision)
+            # tolerance is an initialize() parameter
+            solver.initialize(viscosity=s["eta"], hydrodynamicRadius=s["a"],
+                              includeAngular=bool(s["ang"]), tolerance=run["tol"])
+            solver.setPositions(pos)
+            for call in range(3):
+                zz = z[run["tag"] + "_z"][call]
+                u, w, it, res = solver.sqrtMdotW_noise(zz)
+                y = np.concatenate([u.ravel(), w.ravel()]) if s["ang"] else u.ravel()
+                yr = z[run["tag"] + "_y"][call]
+                rel = np.linalg.norm(y - yr) / np.linalg.norm(yr)
+                it_ref = z[run["tag"] + "_it"][call]
+                if precision == "double":
+                    assert it == it_ref, (si, call, it, it_ref)
+                    assert rel < 1e-8, (si, call, rel)
+                else:
+                    assert abs(it - it_ref) <= 1, (si, call, it, it_ref)
+                    assert rel < 10 * run["tol"], (si, call, rel)
+                assert res <= run["tol"]
+
+
+@pytest.mark.parametrize("wall", [0, 1])
+def test_matches_oracle_restatement_and_exact_root(cuda, oracle, wall):
+    rng = np.random.default_rng(21 + wall)
+    N = 200
+    p = rng.uniform(0, 25, (N, 3))
+    if wall:
+        p[:, 2] = rng.uniform(1.5, 10, N)
+    a, eta = 1.0, 1 / (6 * np.pi)
+    M = oracle.dense(p, a=a, viscosity=eta, wall=wall, include_angular=True)
+    S = oracle.sqrtm_dense(M)
+    ref = oracle.Lanczos()
+    for precision, tol in (("double", 1e-8), ("float", 1e-6)):
+        s = make_solver(wall, 1, a, eta, precision)
+        s.initialize(viscosity=eta, hydrodynamicRadius=a, includeAngular=True, tolerance=tol)
+        s.setPositions(p)
+        zz = rng.normal(size=6 * N)
+        u, w, it, res = s.sqrtMdotW_noise(zz, prefactor=1.0)
+        y = np.concatenate([u.ravel(), w.ravel()])
+        ex = S @ zz
+        assert np.linalg.norm(y - ex) / np.linalg.norm(ex) < 20 * tol
+        yo, ito = oracle.Lanczos().run(lambda v: M @ v, zz, tol)
+        assert abs(it - ito) <= 1
+
+
+def _ks_fdt(M, draw):
+    """fluctuation_dissipation_KS of the reference tests."""
+    from scipy.stats import kstest, norm
+    lam, Q = np.linalg.eigh(M)
+    inv_half = (Q / np.sqrt(np.clip(lam, 1e-300, None))).T
+    n = lam.size
+    mu_alpha = 0.999 ** (1 / n)
+    Ns = int(round(2 * (norm.ppf(mu_alpha) / 0.05) ** 2))
+    X = np.array([draw() for _ in range(Ns)]).T
+    Y = inv_half @ X
+    for m in range(n):
+        if lam[m] < 1e-6:
+            continue
+        _, pval = kstest(Y[m], "norm")
+        assert pval > 1 - mu_alpha, (m, pval)
+
+
+@pytest.mark.parametrize("pz", ["open", "single_wall"])
+@pytest.mark.parametrize("ang", [False, True])
+@pytest.mark.parametrize("N", [1, 2, 10])
+def test_fluctuation_dissipation(cuda, pz, ang, N):
+    from libmobility_gb300 import NBody
+    s = NBody("open", "open", pz, precision="double")
+    s.setParameters(**({"wallHeight": 0.0} if pz == "single_wall" else {}))
+    s.initialize(viscosity=1.0, hydrodynamicRadius=0.95, includeAngular=ang, seed=1234 + N)
+    rng = np.random.default_rng(N)
+    p = rng.random((N, 3)) - 0.5
+    p[:, 2] += 0.5
+    s.setPositions(p * 10)
+    M = compute_M(s, N, ang)
+
+    def draw():
+        u, w = s.sqrtMdotW(prefactor=1.0)
+        return np.concatenate([u.ravel(), w.ravel()]) if ang else u.ravel()
+
+    _ks_fdt(M, draw)
+
+
+@pytest.mark.parametrize("ang", [False, True])
+def test_prefactor_and_seed(cuda, ang):
+    from libmobility_gb300 import NBody
+    out = []
+    for pf in (2.45, 1.0):
+        s = NBody("open", "open", "single_wall")
+        s.setParameters(wallHeight=0.0)
+        s.initialize(viscosity=1.0, hydrodynamicRadius=1.0, includeAngular=ang, seed=4321)
+        s.setPositions(np.array([[1.0, 2.0, 3.0], [2.5, 2.0, 3.5]]))
+        out.append((s.sqrtMdotW(prefactor=pf), s.divM(prefactor=pf)))
+    (a1, d1), (a0, d0) = out
+    assert np.allclose(a1[0], 2.45 * a0[0], atol=1e-4)
+    assert np.allclose(d1[0], 2.45 * d0[0], atol=1e-4)
+    if ang:
+        assert np.allclose(a1[1], 2.45 * a0[1], atol=1e-4)
+        assert np.allclose(d1[1], 2.45 * d0[1], atol=1e-4)
+
+
+def test_callback_and_nonconvergence(cuda):
+    s = make_solver(0, 0, 1.0, 1.0, "float")
+    seen = []
+    s.initialize(viscosity=1.0, hydrodynamicRadius=1.0, tolerance=1e-30,
+                 lanczos_callback=lambda i, e: seen.append((i, e)))
+    s.setPositions(np.random.default_rng(1).random((20, 3)) * 10)
+    with pytest.raises(RuntimeError, match="Could not converge"):
+        s.sqrtMdotW()
+    assert len(seen) == 199 and seen[0][0] == 1
+    # the handle is still usable afterwards
+    s.initialize(viscosity=1.0, hydrodynamicRadius=1.0, tolerance=1e-4)
+    s.setPositions(np.random.default_rng(1).random((20, 3)) * 10)
+    u, _ = s.sqrtMdotW()
+    assert np.isfinite(u).all() and np.abs(u).max() > 0
