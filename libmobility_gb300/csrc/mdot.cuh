@@ -175,14 +175,14 @@ mdot_kernel(const MdotArgs<R> a) {
     int i = tgt0 + threadIdx.x + t * THREADS;
     int ic = i < N ? i : N - 1;
     R x = a.pos[3 * ic], y = a.pos[3 * ic + 1], z = a.pos[3 * ic + 2];
-    xi[t] = x * ia;
-    yi[t] = y * ia;
+    xi[t] = mul_rn(x, ia);
+    yi[t] = mul_rn(y, ia);
     if (GEOM == kWall) {
-      R zs = z * ia;
+      R zs = mul_rn(z, ia);
       bi[t] = zs < R(0) ? R(0) : (zs > R(1) ? R(1) : zs);
       zi[t] = zs > R(1) ? zs : R(1);
     } else {
-      zi[t] = z * ia;
+      zi[t] = mul_rn(z, ia);
       bi[t] = R(1);
     }
     int s = system_of(a, ic);
@@ -216,14 +216,14 @@ mdot_kernel(const MdotArgs<R> a) {
       if (j < c_end) {
         R x = a.pos[3 * j], y = a.pos[3 * j + 1], z = a.pos[3 * j + 2];
         R b = R(1);
-        p.x = x * ia;
-        p.y = y * ia;
+        p.x = mul_rn(x, ia);
+        p.y = mul_rn(y, ia);
         if (GEOM == kWall) {
-          R zs = z * ia;
+          R zs = mul_rn(z, ia);
           b = zs < R(0) ? R(0) : (zs > R(1) ? R(1) : zs);
           p.z = zs > R(1) ? zs : R(1);
         } else {
-          p.z = z * ia;
+          p.z = mul_rn(z, ia);
         }
         if (HAS_F) { fv.x = b * a.F[3 * j]; fv.y = b * a.F[3 * j + 1]; fv.z = b * a.F[3 * j + 2]; }
         if (USE_T) { tv.x = b * a.T[3 * j]; tv.y = b * a.T[3 * j + 1]; tv.z = b * a.T[3 * j + 2]; }

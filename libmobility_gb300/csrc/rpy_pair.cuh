@@ -32,6 +32,13 @@ template <class R> __device__ __forceinline__ R dev_rsqrt(R x);
 template <> __device__ __forceinline__ float dev_rsqrt<float>(float x) { return rsqrtf(x); }
 template <> __device__ __forceinline__ double dev_rsqrt<double>(double x) { return rsqrt(x); }
 
+// Multiplication that the compiler may not contract into an FMA with a
+// following subtraction: targets and sources are scaled by 1/a with it, so a
+// particle paired with itself (or with a coincident one) yields exactly d = 0.
+template <class R> __device__ __forceinline__ R mul_rn(R a, R b);
+template <> __device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
+template <> __device__ __forceinline__ double mul_rn<double>(double a, double b) { return __dmul_rn(a, b); }
+
 template <class R> __device__ __forceinline__ R dev_div(R a, R b);
 template <> __device__ __forceinline__ float dev_div<float>(float a, float b) { return __fdividef(a, b); }
 template <> __device__ __forceinline__ double dev_div<double>(double a, double b) { return a / b; }
