@@ -81,9 +81,20 @@ const char *lmg_create_error(void);
 /* Frees the handle and everything it owns. */
 lmg_status lmg_destroy(lmg_solver *h);
 
-/* Issue work on this CUDA stream (a cudaStream_t; NULL = the handle's own
- * stream, created on first use). */
+/* Issue the handle's work on this CUDA stream.  cuda_stream is a
+ * cudaStream_t used as given, so NULL/0 is CUDA's default stream;
+ * LMG_OWN_STREAM selects the handle's private non-blocking stream (created on
+ * first use), which is also what a handle uses before this is ever called.
+ * The solver may use one more internal stream for work that overlaps the
+ * matrix-vector products of Lanczos; it is joined back before a call
+ * returns. */
+#define LMG_OWN_STREAM ((void *)(intptr_t)-1)
 lmg_status lmg_set_stream(lmg_solver *h, void *cuda_stream);
+
+/* lanczos::Solver::setIterationHardLimit -- include/lanczos/LanczosAlgorithm.h:
+ * 272-274.  Iteration limit of sqrtMdotW (default 200, at most 250); reaching
+ * it is LMG_ERR_NO_CONVERGENCE ("[Lanczos] Could not converge"). */
+lmg_status lmg_set_lanczos_iteration_limit(lmg_solver *h, int limit);
 
 /* setParametersNBody -- solvers/NBody/mobility.h:78-97 and the Python
  * setParameters of solvers/NBody/python_wrapper.cu:50-61.  algorithm is one

@@ -13,6 +13,7 @@ _PKG = Path(__file__).resolve().parent
 LIB_PATH = Path(os.environ.get("LIBMOBILITY_GB300_LIB", _PKG / "liblmg_gb300.so"))
 
 LMG_OK = 0
+LMG_OWN_STREAM = ctypes.c_void_p(2**64 - 1)
 STATUS_NAMES = {
     0: "LMG_OK", 1: "LMG_ERR_INVALID_ARGUMENT", 2: "LMG_ERR_NOT_INITIALIZED",
     3: "LMG_ERR_NO_POSITIONS", 4: "LMG_ERR_BELOW_WALL", 5: "LMG_ERR_NO_CONVERGENCE",
@@ -32,6 +33,7 @@ SIGNATURES = {
     "lmg_create_error": (ctypes.c_char_p, []),
     "lmg_destroy": (_I, [_VP]),
     "lmg_set_stream": (_I, [_VP, _VP]),
+    "lmg_set_lanczos_iteration_limit": (_I, [_VP, _I]),
     "lmg_set_parameters_nbody": (_I, [_VP, ctypes.c_char_p, _I, _I, _I, _D, _D]),
     "lmg_initialize": (_I, [_VP, _D, _D, _I, _D, ctypes.c_uint64, LANCZOS_CALLBACK, _VP]),
     "lmg_set_positions": (_I, [_VP, _VP, _SZ]),

@@ -73,7 +73,16 @@ lmg_status lmg_destroy(lmg_solver *h) {
 }
 
 lmg_status lmg_set_stream(lmg_solver *h, void *s) {
-  return guarded(h, [&](lmg::SolverBase &m) { m.set_stream((cudaStream_t)s); });
+  return guarded(h, [&](lmg::SolverBase &m) {
+    if (s == LMG_OWN_STREAM)
+      m.use_own_stream();
+    else
+      m.set_stream((cudaStream_t)s);
+  });
+}
+
+lmg_status lmg_set_lanczos_iteration_limit(lmg_solver *h, int limit) {
+  return guarded(h, [&](lmg::SolverBase &m) { m.set_iteration_limit(limit); });
 }
 
 lmg_status lmg_set_parameters_nbody(lmg_solver *h, const char *algorithm, int Nbatch,

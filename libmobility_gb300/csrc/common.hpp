@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <stdexcept>
 #include <string>
 
@@ -72,6 +73,35 @@ template <class T> struct PinnedBuffer {
   void release() {
     if (ptr) cudaFreeHost(ptr);
     ptr = nullptr;
+    count = 0;
+  }
+};
+
+// Page-locked host allocation mapped into the device address space: small
+// results written by kernels (Lanczos scalars) are read by the host after an
+// event, without a copy operation.
+template <class T> struct MappedBuffer {
+  T *ptr = nullptr;
+  T *dptr = nullptr;
+  size_t count = 0;
+  MappedBuffer() = default;
+  MappedBuffer(const MappedBuffer &) = delete;
+  MappedBuffer &operator=(const MappedBuffer &) = delete;
+  ~MappedBuffer() { release(); }
+  T *ensure(size_t n) {
+    if (n > count) {
+      release();
+      LMG_CUDA(cudaHostAlloc((void **)&ptr, n * sizeof(T), cudaHostAllocMapped));
+      LMG_CUDA(cudaHostGetDevicePointer((void **)&dptr, ptr, 0));
+      std::memset(ptr, 0, n * sizeof(T));
+      count = n;
+    }
+    return ptr;
+  }
+  T *device_ptr() const { return dptr; }
+  void release() {
+    if (ptr) cudaFreeHost(ptr);
+    ptr = dptr = nullptr;
     count = 0;
   }
 };

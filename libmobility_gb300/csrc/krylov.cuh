@@ -10,8 +10,11 @@
 //   err = |y_i - y_{i-1}| / |y_{i-1}|              computeError :202-222
 // GB300 choices: the Krylov vectors stay in the solver precision, every inner
 // product and norm accumulates in FP64 and the scalars alpha, beta, |z| live in
-// device memory as FP64 (no host round trip per iteration); T_m^{1/2} e1 is
-// computed on the device in FP64 by implicit QL (below).
+// device memory as FP64.  The m x m tridiagonal eigen-problem behind
+// T_m^{1/2} e1 (m <= 250) is solved in FP64 by implicit QL (below) on the Grace
+// host core, whose scalar FP64 latency is far below that of GB300's narrow FP64
+// units; alpha/beta reach it through mapped host memory while the GPU already
+// runs the next matrix-vector product.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -203,7 +206,7 @@ __global__ void krylov_alpha_kernel(R *w, const R *vi, const R *vprev, size_t n,
 // w -= alpha_i v_i;  beta_i = |w| with the breakdown rule
 template <class R>
 __global__ void krylov_beta_kernel(R *w, const R *vi, size_t n, int i, double *partials,
-                                   unsigned *ticket, KrylovScalars *sc) {
+                                   unsigned *ticket, KrylovScalars *sc, double *host_ab) {
   const R al = (R)sc->alpha[i];
   double v[1] = {0.0};
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
@@ -218,6 +221,9 @@ __global__ void krylov_beta_kernel(R *w, const R *vi, size_t n, int i, double *p
     const double tol = 1e-3 * sc->alpha[i] / sc->normz;  // LanczosAlgorithm.cu:141-143
     if (b < tol) b = 0.0;
     sc->beta[i] = b;
+    // (alpha_i, beta_i) for the host-side eigen-solve, in mapped host memory
+    host_ab[2 * i] = sc->alpha[i];
+    host_ab[2 * i + 1] = b;
   }
 }
 
@@ -248,7 +254,18 @@ struct RotLog {
   int capacity;
 };
 
-__host__ __device__ inline int tridiag_sqrt_e1(const double *alpha, const double *beta, int m,
+inline double pythag(double a, double b) {
+  const double r = sqrt(a * a + b * b);
+  if (r == 0.0 || isinf(r)) {  // rescale only when the plain form fails
+    const double p = fmax(fabs(a), fabs(b));
+    if (p == 0.0) return 0.0;
+    const double q = fmin(fabs(a), fabs(b)) / p;
+    return p * sqrt(1.0 + q * q);
+  }
+  return r;
+}
+
+inline int tridiag_sqrt_e1(const double *alpha, const double *beta, int m,
                                                double *d, double *e, double *q0, RotLog log,
                                                double *out) {
   for (int k = 0; k < m; k++) {
@@ -270,7 +287,7 @@ __host__ __device__ inline int tridiag_sqrt_e1(const double *alpha, const double
       if (++iter > 60) return 1;
       // Wilkinson-type shift from the leading 2x2 block
       double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-      double r = hypot(g, 1.0);
+      double r = pythag(g, 1.0);
       g = d[mm] - d[l] + e[l] / (g + (g >= 0.0 ? fabs(r) : -fabs(r)));
       double s = 1.0, c = 1.0, p = 0.0;
       int i = mm - 1;
@@ -278,7 +295,7 @@ __host__ __device__ inline int tridiag_sqrt_e1(const double *alpha, const double
       for (; i >= l; i--) {
         double f = s * e[i];
         const double b = c * e[i];
-        r = hypot(f, g);
+        r = pythag(f, g);
         e[i + 1] = r;
         if (r == 0.0) {  // underflow: split the matrix here and restart
           d[i + 1] -= p;
@@ -298,7 +315,8 @@ __host__ __device__ inline int tridiag_sqrt_e1(const double *alpha, const double
         q0[i] = c * a0 - s * a1;
         q0[i + 1] = s * a0 + c * a1;
         if (nrot >= log.capacity) return 2;
-        log.cs[nrot] = make_double2(c, s);
+        log.cs[nrot].x = c;
+        log.cs[nrot].y = s;
         log.idx[nrot] = i;
         nrot++;
       }
@@ -320,18 +338,6 @@ __host__ __device__ inline int tridiag_sqrt_e1(const double *alpha, const double
   return 0;
 }
 
-// One thread: c = T_m^{1/2} e1 (FP64) for m = i+1.
-__global__ void krylov_tridiag_kernel(KrylovScalars *sc, int m, double *work, RotLog log,
-                                      double *c_out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double *d = work, *e = work + m, *q0 = work + 2 * m;
-  const int rc = tridiag_sqrt_e1(sc->alpha, sc->beta, m, d, e, q0, log, c_out);
-  if (rc != 0) {
-    sc->status = rc;
-    for (int k = 0; k < m; k++) c_out[k] = nan("");
-  }
-}
-
 // y = |z| V_m c   (V row-major: row k is v_k, n elements)
 template <class R>
 __global__ void krylov_estimate_kernel(const R *V, size_t ldv, int m, const double *c,
@@ -348,24 +354,23 @@ __global__ void krylov_estimate_kernel(const R *V, size_t ldv, int m, const doub
   }
 }
 
-// err = |y - old| / |old| (FP64), then old = y.  first: only copy.
+// err = |y - yprev| / |yprev| (FP64) -> sc->err and the mapped host copy
 template <class R>
-__global__ void krylov_error_kernel(const R *y, R *old, size_t n, int first, double *partials,
-                                    unsigned *ticket, KrylovScalars *sc) {
+__global__ void krylov_error_kernel(const R *y, const R *yprev, size_t n, double *partials,
+                                    unsigned *ticket, KrylovScalars *sc, double *host_err) {
   double v[2] = {0.0, 0.0};
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
        e += (size_t)gridDim.x * blockDim.x) {
-    const R yo = old[e], yn = y[e];
-    if (!first) {
-      const double a = (double)yo, dlt = (double)yn - (double)yo;
-      v[0] += a * a;
-      v[1] += dlt * dlt;
-    }
-    old[e] = yn;
+    const double a = (double)yprev[e], dlt = (double)y[e] - a;
+    v[0] += a * a;
+    v[1] += dlt * dlt;
   }
-  if (first) return;
   double tot[2];
-  if (grid_sum<2>(v, partials, ticket, tot)) sc->err = fabs(sqrt(tot[1]) / sqrt(tot[0]));
+  if (grid_sum<2>(v, partials, ticket, tot)) {
+    const double err = fabs(sqrt(tot[1]) / sqrt(tot[0]));
+    sc->err = err;
+    *host_err = err;
+  }
 }
 
 // out += pf * y  (used for both the linear and the angular halves)

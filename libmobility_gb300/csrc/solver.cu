@@ -90,7 +90,14 @@ __global__ void add_scaled_diff_kernel(R *out, const R *a, const R *b, size_t n,
 template <class R> class Solver final : public SolverBase {
  public:
   Solver(Periodicity x, Periodicity y, Periodicity z) : SolverBase(x, y, z) {}
-  ~Solver() override { release_all(); }
+  ~Solver() override {
+    release_all();
+    for (auto &e : ev_iter_)
+      if (e) cudaEventDestroy(e);
+    if (ev_check_) cudaEventDestroy(ev_check_);
+    if (ev_side_) cudaEventDestroy(ev_side_);
+    if (side_) cudaStreamDestroy(side_);
+  }
 
   const char *precision() const override { return sizeof(R) == 4 ? "float" : "double"; }
 
@@ -113,13 +120,17 @@ template <class R> class Solver final : public SolverBase {
   DeviceBuffer<unsigned> red_ticket_;     // reduction ticket (self-resetting)
   DeviceBuffer<double> dmin_;
   // Lanczos
-  DeviceBuffer<R> V_, w_, y_, old_, z_;
+  DeviceBuffer<R> V_, w_, y_, ybuf_, z_;
   DeviceBuffer<KrylovScalars> sc_;
-  DeviceBuffer<double> cvec_, qlwork_;
-  DeviceBuffer<double2> rot_cs_;
-  DeviceBuffer<int> rot_idx_;
-  PinnedBuffer<KrylovScalars> h_sc_;
+  DeviceBuffer<double> cvec_;
+  MappedBuffer<double> mirror_;       // (alpha_i, beta_i) pairs + err, device-written
+  PinnedBuffer<double> hc_;           // T^{1/2} e1 staged for the device (2 slots)
+  std::vector<double> ql_work_;       // host QL work arrays
+  std::vector<double2> rot_cs_;       // host QL rotation log
+  std::vector<int> rot_idx_;
   PinnedBuffer<double> h_dbl_;
+  cudaStream_t side_ = nullptr;       // high-priority stream for per-check work
+  cudaEvent_t ev_iter_[2] = {nullptr, nullptr}, ev_check_ = nullptr, ev_side_ = nullptr;
   // RFD
   DeviceBuffer<R> rfd_noise_, rfd_pos_, rfd_mp_, rfd_mm_;
   int num_sms_ = 0;
@@ -134,6 +145,8 @@ template <class R> class Solver final : public SolverBase {
     return (int)std::max<size_t>(1, std::min(b, cap));
   }
   void ensure_reduction(int blocks);
+  size_t red_half() const { return red_part_.count / 2; }
+  void ensure_side();
   const R *device_input(const void *p, size_t n, R *stage);
   // M . [F;T] on device buffers: the Lanczos matvec and the RFD probes
   void mdot_device(const R *pos, const R *F, const R *T, R *U, R *W);
@@ -152,15 +165,16 @@ template <class R> int Solver<R>::sms() {
 template <class R> void Solver<R>::release_all() {
   pos_.release(); pos_tmp_.release(); in_stage_.release(); out_stage_.release(); pin_.release();
   part_.release(); tickets_.release(); red_part_.release(); red_ticket_.release(); dmin_.release();
-  V_.release(); w_.release(); y_.release(); old_.release(); z_.release(); sc_.release();
-  cvec_.release(); qlwork_.release(); rot_cs_.release(); rot_idx_.release(); h_sc_.release();
+  V_.release(); w_.release(); y_.release(); ybuf_.release(); z_.release(); sc_.release();
+  cvec_.release(); mirror_.release(); hc_.release(); ql_work_ = {}; rot_cs_ = {}; rot_idx_ = {};
   h_dbl_.release(); rfd_noise_.release(); rfd_pos_.release(); rfd_mp_.release(); rfd_mm_.release();
   plans_.clear();
   tickets_zeroed_ = false;
 }
 
 template <class R> void Solver<R>::ensure_reduction(int blocks) {
-  red_part_.ensure((size_t)4 * std::max(blocks, 1024));
+  // two halves: the solver stream and the side stream reduce independently
+  red_part_.ensure((size_t)8 * std::max(blocks, 1024));
   if (!red_ticket_.ptr) {
     red_ticket_.ensure(4);
     LMG_CUDA(cudaMemsetAsync(red_ticket_.ptr, 0, 4 * sizeof(unsigned), stream()));
@@ -322,71 +336,135 @@ void Solver<R>::mdot(const void *F, size_t nF, const void *T, size_t nT, void *U
   }
 }
 
-// Lanczos to tolerance; returns the iteration index at convergence.
+template <class R> void Solver<R>::ensure_side() {
+  if (!side_) {
+    int lo = 0, hi = 0;
+    LMG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    LMG_CUDA(cudaStreamCreateWithPriority(&side_, cudaStreamNonBlocking, hi));
+    for (auto &e : ev_iter_) LMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    LMG_CUDA(cudaEventCreateWithFlags(&ev_check_, cudaEventDisableTiming));
+    LMG_CUDA(cudaEventCreateWithFlags(&ev_side_, cudaEventDisableTiming));
+  }
+}
+
+// Lanczos to tolerance (LanczosAlgorithm.cu:173-200); returns the iteration
+// index at convergence and leaves y = sqrt(M) z in *y_out.
+//
+// Schedule per iteration i on the solver stream S: matvec, alpha, beta (which
+// also writes alpha_i, beta_i to mapped host memory), next -> event I_i.  The
+// GPU is kept one iteration ahead: iteration i+1 is issued before the host
+// handles the convergence check of iteration i.  A check (every i >= k, the
+// adaptive start of LanczosAlgorithm.cu:179-184, or every i with a callback)
+// waits for I_i, solves the FP64 tridiagonal problem on the host while the
+// GPU runs iteration i+1, then on the high-priority side stream P computes
+// y_i = |z| V c_i and |y_i - y_{i-1}| / |y_{i-1}|, and reads the error back.
+// At the first check of a solve there is no y_{i-1}; its error counts as
+// infinite (the reference compares against a zero or stale buffer there).
 template <class R>
-int Solver<R>::lanczos(const R *z, R *y, size_t n, double tol, double *residual) {
+int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *residual) {
   const int limit = hard_limit_;
   const int blocks = vec_blocks(n);
   ensure_reduction(blocks);
+  ensure_side();
   R *V = V_.ensure((size_t)(limit + 1) * n);
   R *w = w_.ensure(n);
-  R *old = old_.ensure(n);
+  R *yb = ybuf_.ensure(2 * n);
   KrylovScalars *sc = sc_.ensure(1);
-  double *c = cvec_.ensure(256);
-  double *work = qlwork_.ensure(3 * 256);
-  const int rot_cap = 64 * limit * limit;
-  RotLog log{rot_cs_.ensure(rot_cap), rot_idx_.ensure(rot_cap), rot_cap};
-  KrylovScalars *hsc = h_sc_.ensure(1);
+  double *cdev = cvec_.ensure(2 * kMaxLanczosIterations);
+  double *mir = mirror_.ensure(2 * 256 + 8);  // [2i] alpha_i, [2i+1] beta_i, [512] err
+  double *mir_dev = mirror_.device_ptr();
+  double *hc = hc_.ensure(2 * kMaxLanczosIterations);
+  const int rot_cap = 24 * limit * limit + 1024;
+  if ((int)rot_cs_.size() < rot_cap) {
+    rot_cs_.resize(rot_cap);
+    rot_idx_.resize(rot_cap);
+  }
+  ql_work_.resize(3 * 256);
+  RotLog log{rot_cs_.data(), rot_idx_.data(), rot_cap};
   cudaStream_t st = stream();
-  unsigned *tk = red_ticket_.ptr;
-  double *rp = red_part_.ptr;
+  cudaStream_t sd = side_;
+  unsigned *tk = red_ticket_.ptr, *tk_side = red_ticket_.ptr + 1;
+  double *rp = red_part_.ptr, *rp_side = red_part_.ptr + red_half();
+  const size_t n3 = 3 * (size_t)N_;
+
   LMG_CUDA(cudaMemsetAsync(sc, 0, sizeof(KrylovScalars), st));
   krylov_norm_kernel<R><<<blocks, kRedThreads, 0, st>>>(z, n, rp, tk, sc);
   count_launch();
   krylov_scale_first_kernel<R><<<blocks, kRedThreads, 0, st>>>(z, V, n, sc);
   count_launch();
-  LMG_CUDA(cudaGetLastError());
-  const size_t n3 = 3 * (size_t)N_;
-  const int k = std::min(check_steps_, limit - 2);
-  for (int i = 0; i < limit; i++) {
-    R *vi = V + (size_t)i * n;
-    // w = M v_i  ([F;T] halves of the Krylov vector)
-    mdot_device(pos_.ptr, vi, ang_ ? vi + n3 : nullptr, w, ang_ ? w + n3 : nullptr);
-    krylov_alpha_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vi, i > 0 ? vi - n : vi, n, i, rp,
+
+  auto issue = [&](int j) {
+    R *vj = V + (size_t)j * n;
+    mdot_device(pos_.ptr, vj, ang_ ? vj + n3 : nullptr, w, ang_ ? w + n3 : nullptr);
+    krylov_alpha_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vj, j > 0 ? vj - n : vj, n, j, rp,
                                                            tk, sc);
     count_launch();
-    krylov_beta_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vi, n, i, rp, tk, sc);
+    krylov_beta_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vj, n, j, rp, tk, sc, mir_dev);
     count_launch();
-    krylov_next_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vi + n, n, i, sc);
+    krylov_next_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vj + n, n, j, sc);
     count_launch();
-    if (i >= k || cb_ != nullptr) {
-      const int m = i + 1;
-      krylov_tridiag_kernel<<<1, 32, 0, st>>>(sc, m, work, log, c);
+    LMG_CUDA(cudaEventRecord(ev_iter_[j & 1], st));
+  };
+
+  const int k = std::min(check_steps_, limit - 2);
+  std::vector<double> al(limit), be(limit);
+  issue(0);
+  bool have_prev = false;
+  int done = -1;
+  double err = 0;
+  for (int i = 0; i < limit; i++) {
+    if (i + 1 < limit) issue(i + 1);
+    if (!(i >= k || cb_ != nullptr)) continue;
+    const int m = i + 1;
+    LMG_CUDA(cudaEventSynchronize(ev_iter_[i & 1]));
+    for (int q = 0; q < m; q++) {
+      al[q] = mir[2 * q];
+      be[q] = mir[2 * q + 1];
+    }
+    double *c = hc + (i & 1) * kMaxLanczosIterations;
+    const int rc = tridiag_sqrt_e1(al.data(), be.data(), m, ql_work_.data(),
+                                   ql_work_.data() + 256, ql_work_.data() + 512, log, c);
+    if (rc != 0)
+      for (int q = 0; q < m; q++) c[q] = std::nan("");
+    double *cd = cdev + (i & 1) * kMaxLanczosIterations;
+    R *yi = yb + (size_t)(i & 1) * n;
+    LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i & 1], 0));
+    LMG_CUDA(cudaMemcpyAsync(cd, c, m * sizeof(double), cudaMemcpyHostToDevice, sd));
+    krylov_estimate_kernel<R><<<blocks, kRedThreads, 0, sd>>>(V, n, m, cd, sc, yi, n);
+    count_launch();
+    if (have_prev) {
+      krylov_error_kernel<R><<<blocks, kRedThreads, 0, sd>>>(
+          yi, yb + (size_t)((i + 1) & 1) * n, n, rp_side, tk_side, sc, mir_dev + 512);
       count_launch();
-      krylov_estimate_kernel<R><<<blocks, kRedThreads, 0, st>>>(V, n, m, c, sc, y, n);
-      count_launch();
-      krylov_error_kernel<R><<<blocks, kRedThreads, 0, st>>>(y, old, n, i == 0 ? 1 : 0, rp, tk,
-                                                             sc);
-      count_launch();
-      LMG_CUDA(cudaGetLastError());
-      if (i > 0) {
-        LMG_CUDA(cudaMemcpyAsync(hsc, sc, 2 * sizeof(double) + 2 * sizeof(int),
-                                 cudaMemcpyDeviceToHost, st));
-        LMG_CUDA(cudaStreamSynchronize(st));
-        const double err = hsc->err;
-        if (residual) *residual = err;
-        if (std::isnan(err) || hsc->status != 0)
-          throw Error(LMG_ERR_NAN, "[Lanczos] Unknown error (found NaN in result guess)");
-        if (cb_) cb_(i, err, cb_user_);
-        if (err <= tol) {
-          lanczos_register(i);
-          return i;
-        }
-      }
+    }
+    LMG_CUDA(cudaEventRecord(ev_check_, sd));
+    LMG_CUDA(cudaGetLastError());
+    LMG_CUDA(cudaEventSynchronize(ev_check_));
+    err = have_prev ? mir[512] : HUGE_VAL;
+    if (have_prev) {  // the reference never tests the first estimate (i > 0 there)
+      if (residual) *residual = err;
+      if (std::isnan(err))
+        throw Error(LMG_ERR_NAN, "[Lanczos] Unknown error (found NaN in result guess)");
+    }
+    if (cb_ && i > 0) cb_(i, err, cb_user_);
+    const bool tested = have_prev;
+    have_prev = true;
+    if (tested && err <= tol) {
+      lanczos_register(i);
+      done = i;
+      break;
     }
   }
-  LMG_CUDA(cudaStreamSynchronize(st));
-  throw Error(LMG_ERR_NO_CONVERGENCE, "[Lanczos] Could not converge");
+  if (done < 0) {
+    LMG_CUDA(cudaStreamSynchronize(st));
+    throw Error(LMG_ERR_NO_CONVERGENCE, "[Lanczos] Could not converge");
+  }
+  // the caller's stream sees the result after the side stream's last work
+  LMG_CUDA(cudaMemcpyAsync(y_out, yb + (size_t)(done & 1) * n, n * sizeof(R),
+                           cudaMemcpyDeviceToDevice, sd));
+  LMG_CUDA(cudaEventRecord(ev_side_, sd));
+  LMG_CUDA(cudaStreamWaitEvent(st, ev_side_, 0));
+  return done;
 }
 
 template <class R>
@@ -551,11 +629,12 @@ void Solver<R>::div_m(void *U, size_t nU, void *W, size_t nW, double prefactor) 
 template <class R> void Solver<R>::clean() {
   // Mobility::clean drops the Lanczos object (its engine and check schedule)
   // and its storage; positions and parameters stay.
-  if (stream_) cudaStreamSynchronize(stream_);
+  if (have_stream_) cudaStreamSynchronize(stream_);
+  if (side_) cudaStreamSynchronize(side_);
   lanczos_alive_ = false;
   check_steps_ = 3;
-  V_.release(); w_.release(); y_.release(); old_.release(); z_.release();
-  rot_cs_.release(); rot_idx_.release();
+  V_.release(); w_.release(); y_.release(); ybuf_.release(); z_.release();
+  rot_cs_ = {}; rot_idx_ = {};
   part_.release(); tickets_.release(); tickets_zeroed_ = false; plans_.clear();
   rfd_noise_.release(); rfd_pos_.release(); rfd_mp_.release(); rfd_mm_.release();
 }

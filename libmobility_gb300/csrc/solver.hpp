@@ -18,6 +18,10 @@
 
 namespace lmg {
 
+// Size of the FP64 scalar arrays of a Lanczos solve (the iteration limit can
+// be raised up to this; the reference default is 200).
+constexpr int kMaxLanczosIterations = 250;
+
 enum class Periodicity { single_wall, two_walls, open, periodic, unspecified };
 
 Periodicity parse_periodicity(const std::string &s);  // pythonify.h:38-52
@@ -49,8 +53,10 @@ class SolverBase {
 
   int64_t number_particles() const { return N_; }
   bool include_angular() const { return ang_; }
-  void set_stream(cudaStream_t s);
+  void set_stream(cudaStream_t s);   // s is used as given (0 = default stream)
+  void use_own_stream();
   cudaStream_t stream();
+  void set_iteration_limit(int limit);  // lanczos::Solver::setIterationHardLimit
   void synchronize();
 
   std::string last_error;
@@ -79,10 +85,12 @@ class SolverBase {
   int64_t N_ = 0;
   int batch_count() const { return nbatch_ < 0 ? 1 : nbatch_; }
   int batch_size() const { return nper_ < 0 ? (int)N_ : nper_; }
-  // stream
+  // stream: the caller's (set_stream, 0 = CUDA default stream) or, until
+  // one is set, a private non-blocking stream created on first use
   cudaStream_t stream_ = nullptr;
+  bool have_stream_ = false;
   bool own_stream_ = false;
-  bool user_stream_ = false;
+  cudaStream_t own_ = nullptr;
 
   // shared argument checks (messages of pythonify.h / mobility.h)
   void check_positions_set(const char *who) const;

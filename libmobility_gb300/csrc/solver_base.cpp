@@ -30,7 +30,7 @@ SolverBase::SolverBase(Periodicity x, Periodicity y, Periodicity z) {
 }
 
 SolverBase::~SolverBase() {
-  if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+  if (own_) cudaStreamDestroy(own_);
 }
 
 void SolverBase::set_parameters(int nbatch, int nper, std::optional<double> wall_height,
@@ -142,27 +142,37 @@ void SolverBase::langevin(double dt, double kbt, const void *F, size_t nF, const
 }
 
 void SolverBase::set_stream(cudaStream_t s) {
-  if (s) {
-    if (own_stream_ && stream_) cudaStreamDestroy(stream_);
-    own_stream_ = false;
-    stream_ = s;
-    user_stream_ = true;
-  } else if (user_stream_) {
-    stream_ = nullptr;
-    user_stream_ = false;
-  }
+  stream_ = s;
+  have_stream_ = true;
+  own_stream_ = false;
+}
+
+void SolverBase::use_own_stream() {
+  have_stream_ = false;
+  own_stream_ = false;
 }
 
 cudaStream_t SolverBase::stream() {
-  if (!stream_) {
-    LMG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  if (!have_stream_) {
+    if (!own_) LMG_CUDA(cudaStreamCreateWithFlags(&own_, cudaStreamNonBlocking));
+    stream_ = own_;
+    have_stream_ = true;
     own_stream_ = true;
   }
   return stream_;
 }
 
+// LanczosAlgorithm.h:272-274 (the reference default is 200)
+void SolverBase::set_iteration_limit(int limit) {
+  if (limit < 3 || limit > kMaxLanczosIterations)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] the Lanczos iteration limit must be in [3, " +
+                    std::to_string(kMaxLanczosIterations) + "]");
+  hard_limit_ = limit;
+}
+
 void SolverBase::synchronize() {
-  if (stream_) LMG_CUDA(cudaStreamSynchronize(stream_));
+  if (have_stream_) LMG_CUDA(cudaStreamSynchronize(stream_));
 }
 
 }  // namespace lmg

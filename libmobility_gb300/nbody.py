@@ -137,18 +137,23 @@ class NBody:
         return r if r.size else None
 
     def _bind_stream(self, *objs):
-        """Order the work after the caller's torch stream when CUDA tensors
-        (inputs as _Arr, or output tensors) are involved; otherwise use the
-        handle's own stream."""
-        stream = None
+        """Issue the work on the caller's current torch stream when CUDA
+        tensors (inputs as _Arr, or output tensors) are involved, so it is
+        ordered with the caller's own work (the default stream included);
+        otherwise on the handle's private stream."""
         for x in objs:
             if x is None:
                 continue
             cuda = x.is_cuda if isinstance(x, _Arr) else (_is_torch(x) and x.is_cuda)
             if cuda:
                 stream = _torch().cuda.current_stream(x.device).cuda_stream
-                break
-        self._check(self._lib.lmg_set_stream(self._h, ctypes.c_void_p(stream)))
+                self._check(self._lib.lmg_set_stream(self._h, ctypes.c_void_p(stream)))
+                return
+        self._check(self._lib.lmg_set_stream(self._h, _capi.LMG_OWN_STREAM))
+
+    def setLanczosIterationLimit(self, limit):
+        """lanczos::Solver::setIterationHardLimit (LanczosAlgorithm.h:272-274)."""
+        self._check(self._lib.lmg_set_lanczos_iteration_limit(self._h, int(limit)))
 
     def _zeros(self, shape, framework, device):
         if framework == "torch":

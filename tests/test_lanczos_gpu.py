@@ -131,18 +131,42 @@ def test_prefactor_and_seed(cuda, ang):
 
 
 def test_callback_and_nonconvergence(cuda):
+    """Reaching the iteration limit (setIterationHardLimit of the reference
+    solver) raises "Could not converge" and leaves the handle usable; the
+    callback sees every check from iteration 1 on."""
     s = make_solver(0, 0, 1.0, 1.0, "float")
     seen = []
-    s.initialize(viscosity=1.0, hydrodynamicRadius=1.0, tolerance=1e-30,
+    s.initialize(viscosity=1.0, hydrodynamicRadius=1.0, tolerance=1e-12,
                  lanczos_callback=lambda i, e: seen.append((i, e)))
-    # 300 particles: the Krylov space (900) is not exhausted in 200 steps and
-    # the FP32 rounding keeps the successive-iterate error above 1e-30
     s.setPositions(np.random.default_rng(1).random((300, 3)) * 30)
+    s.setLanczosIterationLimit(6)
     with pytest.raises(RuntimeError, match="Could not converge"):
         s.sqrtMdotW()
-    assert len(seen) == 199 and seen[0][0] == 1
-    # the handle is still usable afterwards
+    assert [i for i, _ in seen] == [1, 2, 3, 4, 5]
+    with pytest.raises(RuntimeError):
+        s.setLanczosIterationLimit(1000)
+    s.setLanczosIterationLimit(200)
     s.initialize(viscosity=1.0, hydrodynamicRadius=1.0, tolerance=1e-4)
     s.setPositions(np.random.default_rng(1).random((20, 3)) * 10)
     u, _ = s.sqrtMdotW()
     assert np.isfinite(u).all() and np.abs(u).max() > 0
+
+
+def test_adaptive_check_schedule_matches_reference(cuda, oracle):
+    """Without a callback the first convergence check moves with the
+    iterations the previous solves needed (LanczosAlgorithm.cu:224-232); the
+    iteration counts over a sequence of solves equal the oracle's, which
+    follows the same schedule."""
+    rng = np.random.default_rng(8)
+    N = 40
+    p = rng.uniform(0, 12, (N, 3))
+    M = oracle.dense(p, a=1.0, viscosity=1.0, include_angular=False)
+    s = make_solver(0, 0, 1.0, 1.0, "double")
+    s.initialize(viscosity=1.0, hydrodynamicRadius=1.0, tolerance=1e-6)
+    s.setPositions(p)
+    ref = oracle.Lanczos()
+    for _ in range(6):
+        zz = rng.normal(size=3 * N)
+        _, _, it, _ = s.sqrtMdotW_noise(zz)
+        _, ito = ref.run(lambda v: M @ v, zz, 1e-6)
+        assert it == ito

@@ -129,6 +129,27 @@ def test_torch_cuda_buffers_and_stream(cuda, oracle):
     assert rel_err(W.cpu().numpy(), Wo) <= 1e-5
 
 
+def test_ordered_on_callers_stream(cuda, oracle):
+    """Results are ordered on the caller's current torch stream (the default
+    stream included): reading them right away, without a synchronize, sees
+    the finished values."""
+    import torch
+    rng = np.random.default_rng(12)
+    N = 4096
+    p = _system(rng, N, 0)
+    F = rng.normal(size=(N, 3))
+    s = make_solver(0, 0, 1.0, 1.0, "float")
+    s.setPositions(torch.tensor(p, device="cuda"))
+    dF = torch.tensor(F, device="cuda", dtype=torch.float32)
+    Uo, _ = oracle.mdot(p, F, None, a=1.0, viscosity=1.0, rows=(0, 256))
+    for stream in (torch.cuda.default_stream(), torch.cuda.Stream()):
+        with torch.cuda.stream(stream):
+            U, _ = s.Mdot(dF)
+            V = U[:256].clone() * 1.0  # consumer on the same stream
+        stream.synchronize()
+        assert rel_err(V.cpu().numpy(), Uo) <= 1e-5
+
+
 def test_no_forces_no_torques_and_overwrite(cuda):
     s = make_solver(0, 1, 1.0, 1.0, "float")
     s.setPositions(np.random.rand(5, 3) * 5)
