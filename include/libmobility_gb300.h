@@ -170,6 +170,29 @@ lmg_status lmg_synchronize(lmg_solver *h);
  * MobilityInterface.h:73-77). */
 const char *lmg_precision_name(const lmg_solver *h);
 
+/* No counterpart in the reference.  Mdot (FP32) that allocates nothing, for
+ * callers that may not allocate device memory: programs whose device memory is
+ * owned by their own pool with no other allocations allowed, or loops that
+ * cannot take the device-wide synchronisation of cudaMalloc/cudaFree.  No
+ * handle: every input and output is a caller-owned DEVICE buffer of 3N floats
+ * (positions measured from the wall, z = 0 at the wall, when single_wall;
+ * no below-the-wall check is made); F or T may be NULL, W is required with
+ * includeAngular; U and W are overwritten as by lmg_mdot.  NperBatch <= 0
+ * means one batch.  The kernel's scratch is a static device array of
+ * LMG_MDOT_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library;
+ * numberParticles above LMG_MDOT_NOALLOC_MAX_PARTICLES is rejected.  The first
+ * call on a device sets up the scratch address (make it before any stream
+ * capture); calls share the scratch, so calls that overlap on the GPU race.
+ * Work is issued on cuda_stream (0 = default stream), nothing is synchronised.
+ * On failure a message is written to err (err_len bytes, may be NULL). */
+#define LMG_MDOT_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)
+#define LMG_MDOT_NOALLOC_MAX_PARTICLES ((int64_t)1 << 24)
+lmg_status lmg_mdot_noalloc_f32(const float *pos, const float *F, const float *T,
+                                float *U, float *W, int64_t numberParticles,
+                                int64_t NperBatch, int single_wall, double viscosity,
+                                double hydrodynamicRadius, int includeAngular,
+                                void *cuda_stream, char *err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,6 +26,7 @@ UNITS = [
     ("mdot_launch.cu", ["-DLMG_REAL=double"], "mdot_d.o"),
     ("solver.cu", [], "solver.o"),
     ("probes.cu", [], "probes.o"),
+    ("noalloc.cu", [], "noalloc.o"),
     ("solver_base.cpp", [], "solver_base.o"),
     ("capi.cpp", [], "capi.o"),
 ]

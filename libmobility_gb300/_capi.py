@@ -48,6 +48,8 @@ SIGNATURES = {
     "lmg_clean": (_I, [_VP]),
     "lmg_synchronize": (_I, [_VP]),
     "lmg_precision_name": (ctypes.c_char_p, [_VP]),
+    "lmg_mdot_noalloc_f32": (_I, [_VP, _VP, _VP, _VP, _VP, ctypes.c_int64, ctypes.c_int64, _I,
+                                 _D, _D, _I, _VP, ctypes.c_char_p, _SZ]),
 }
 
 _lib = None
