@@ -76,6 +76,8 @@ def load():
     lib.lmg_internal_launch_count.argtypes = []
     lib.lmg_internal_fma_probe.restype = _I
     lib.lmg_internal_fma_probe.argtypes = [_I, _I, _I, _VP, _VP]
+    lib.lmg_internal_fma2_probe.restype = _I
+    lib.lmg_internal_fma2_probe.argtypes = [_I, _I, _I, _VP, _VP]
     _lib = lib
     return lib
 

@@ -36,6 +36,25 @@ __global__ void fma_chain_kernel(int iters, float *sink) {
   for (int k = 0; k < 8; k++) s += a[k];
   if (s == -1.0f) sink[threadIdx.x] = s;
 }
+// Same with packed FP32 (fma.rn.f32x2 through __ffma2_rn): 4 independent
+// float2 chains, so the same 8 FMAs per round per thread.
+__global__ void fma2_chain_kernel(int iters, float *sink) {
+  float2 a[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) a[k] = make_float2((threadIdx.x + k) * 1e-7f, k * 1e-7f);
+  const float2 b = make_float2(0.999999f, 0.999999f), c = make_float2(1e-8f, 1e-8f);
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) a[k] = __ffma2_rn(a[k], b, c);
+    }
+  }
+  float s = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) s += a[k].x + a[k].y;
+  if (s == -1.0f) sink[threadIdx.x] = s;
+}
 }  // namespace
 
 extern "C" {
@@ -46,6 +65,12 @@ unsigned long long lmg_internal_launch_count(void) { return lmg::g_launches.load
 // blocks * threads * iters * 64 * 2.
 int lmg_internal_fma_probe(int blocks, int threads, int iters, void *sink, void *stream) {
   fma_chain_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, (float *)sink);
+  return (int)cudaGetLastError();
+}
+
+// Packed variant: the same flop count as lmg_internal_fma_probe.
+int lmg_internal_fma2_probe(int blocks, int threads, int iters, void *sink, void *stream) {
+  fma2_chain_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, (float *)sink);
   return (int)cudaGetLastError();
 }
 }
