@@ -180,6 +180,39 @@ def fp32_peak_tflops(lib, torch):
     return best
 
 
+def mdot_kernel_time(torch, s, dF, dT, reps=20):
+    """Average time of one Mdot launch on the device.  The launches are
+    captured in a CUDA graph and replayed between CUDA events on the same
+    stream, so the host-side cost of the Python call does not starve the GPU
+    at small N; if capture is not possible, back-to-back calls are timed."""
+    for _ in range(3):
+        s.Mdot(dF, dT)
+    torch.cuda.synchronize()
+    try:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, capture_error_mode="relaxed"):
+            for _ in range(reps):
+                s.Mdot(dF, dT)
+        g.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.replay()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / reps, "cuda-graph replay of %d Mdot launches" % reps
+    except Exception as exc:  # pragma: no cover - depends on the driver
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            s.Mdot(dF, dT)
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / reps, f"back-to-back calls ({exc.__class__.__name__})"
+
+
 def cpu_baseline(w, pos, F, T, seconds=8.0):
     """FP64 C oracle (all host threads) on a bounded sample of the workload:
     the first R target rows against every source."""
@@ -283,19 +316,8 @@ def run_ours(args, w, ws, rank, local):
     pairs_per_step = pairs * (1 + (it_mean + 1))  # Mdot + (iterations+1) matvecs
     value = pairs_per_step * ws / t_step
 
-    # --- kernel-level figures: Mdot alone, back to back on the same stream ---
-    st = torch.cuda.current_stream()
-    for _ in range(3):
-        s.Mdot(dF, dT)
-    reps = 20
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(st)
-    for _ in range(reps):
-        s.Mdot(dF, dT)
-    e1.record(st)
-    e1.synchronize()
-    t_mdot = e0.elapsed_time(e1) * 1e-3 / reps
+    # --- kernel-level figures: Mdot alone ---
+    t_mdot, kernel_timing = mdot_kernel_time(torch, s, dF, dT)
     # sqrtMdotW alone
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -360,7 +382,8 @@ def run_ours(args, w, ws, rank, local):
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "peak_source": "FP32 FMA-chain probe measured in this run",
-                     "flops_per_pair": fpp},
+                     "flops_per_pair": fpp, "kernel_ms": t_mdot * 1e3,
+                     "kernel_timing": kernel_timing},
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),
         "clocks": clocks,

@@ -47,6 +47,7 @@ template <class R> struct MdotArgs {
   int chunk;             // sources per split (multiple of THREADS)
   R inv_a;               // 1/a
   PairConst<R> k;
+  WallConst kw;          // fused all-blocks wall constants (FP32 path)
   R *part;               // scratch: [tiles][nsplit][2*NC][BT]
   unsigned *ticket;      // scratch: [tiles]
 };
@@ -83,10 +84,18 @@ template <class R, int GEOM, bool HAS_F, bool HAS_T, bool ANG> struct PairKernel
   static constexpr bool UT = HAS_T && ANG;
   static constexpr bool WT = HAS_T && ANG;
 
+  static constexpr bool FUSED_WALL =
+      GEOM == kWall && UF && UT && WT && WF && sizeof(R) == 4;
+
   // Adds the contribution of source (p, f, t) to target (x, y, z).
-  static __device__ __forceinline__ void eval(const PairConst<R> &k, R xi, R yi, R zi,
-                                              const Q4<R> &p, const Q4<R> &fv,
+  static __device__ __forceinline__ void eval(const PairConst<R> &k, const WallConst &kw, R xi,
+                                              R yi, R zi, const Q4<R> &p, const Q4<R> &fv,
                                               const Q4<R> &tv, Vec3<R> &u, Vec3<R> &w) {
+    if constexpr (FUSED_WALL) {
+      wall_pair_fused(k, kw, xi, yi, zi, p.x, p.y, p.z, fv.x, fv.y, fv.z, tv.x, tv.y, tv.z, u,
+                      w);
+      return;
+    }
     const R dx = xi - p.x;
     const R dy = yi - p.y;
     const R dz = zi - p.z;
@@ -241,7 +250,7 @@ mdot_kernel(const MdotArgs<R> a) {
         const Q4<R> fv = HAS_F ? sf[jj] : Q4<R>{0, 0, 0, 0};
         const Q4<R> tv = USE_T ? st[jj] : Q4<R>{0, 0, 0, 0};
 #pragma unroll
-        for (int t = 0; t < TPT; t++) PK::eval(a.k, xi[t], yi[t], zi[t], p, fv, tv, u[t], w[t]);
+        for (int t = 0; t < TPT; t++) PK::eval(a.k, a.kw, xi[t], yi[t], zi[t], p, fv, tv, u[t], w[t]);
       }
     } else {
       for (int jj = 0; jj < n_here; jj++) {
@@ -251,7 +260,7 @@ mdot_kernel(const MdotArgs<R> a) {
         const Q4<R> tv = USE_T ? st[jj] : Q4<R>{0, 0, 0, 0};
 #pragma unroll
         for (int t = 0; t < TPT; t++)
-          if (j >= lo[t] && j < hi[t]) PK::eval(a.k, xi[t], yi[t], zi[t], p, fv, tv, u[t], w[t]);
+          if (j >= lo[t] && j < hi[t]) PK::eval(a.k, a.kw, xi[t], yi[t], zi[t], p, fv, tv, u[t], w[t]);
       }
     }
     // fold the tile's partial sums

@@ -58,8 +58,8 @@ cudaError_t mdot_plan(const MdotShape &s, int N, int max_src_span, int num_sms, 
   per_sm = std::max(per_sm, 1);
   const long want = 2L * num_sms * per_sm;  // two waves worth of CTAs
   int nsplit = (int)std::max(1L, (want + plan.tiles - 1) / plan.tiles);
-  // keep at least two source tiles per split
-  const int max_split = std::max(1, max_src_span / (2 * kThreads));
+  // at least one full source tile per split
+  const int max_split = std::max(1, max_src_span / kThreads);
   nsplit = std::min(nsplit, max_split);
   if (force_split > 0) nsplit = force_split;
   nsplit = std::min(nsplit, 65535);

@@ -178,9 +178,11 @@ extern "C" lmg_status lmg_mdot_noalloc_f32(const float *pos, const float *F, con
   args.N = (int)N;
   args.nper = (int)nper;
   args.inv_a = (float)(1.0 / a);
-  args.k = lmg::make_pair_const<float>(1.0 / (6.0 * M_PI * viscosity * a),
-                                       1.0 / (8.0 * M_PI * viscosity * a * a * a),
-                                       1.0 / (8.0 * M_PI * viscosity * a * a));
+  const double t0 = 1.0 / (6.0 * M_PI * viscosity * a);
+  const double r0 = 1.0 / (8.0 * M_PI * viscosity * a * a * a);
+  const double rt0 = 1.0 / (8.0 * M_PI * viscosity * a * a);
+  args.k = lmg::make_pair_const<float>(t0, r0, rt0);
+  args.kw = lmg::make_wall_const(t0, r0, rt0);
   args.part = plan.nsplit > 1 ? d->partials : nullptr;
   args.ticket = plan.nsplit > 1 ? d->tickets : nullptr;
   e = lmg::mdot_launch<float>(s, args, plan, stream);

@@ -242,4 +242,153 @@ __device__ __forceinline__ void wall_self_ut(R ih, const Vec3<R> &v, Vec3<R> &ou
   out.y -= c * v.x;
 }
 
+// ---------------------------------------------------------------------------
+// All four wall blocks (UF, UT, WT, WF) of one pair in one fused evaluation.
+//
+// Same tensors as the block-by-block functions above, rearranged so the RPY
+// and image parts share work:
+//   * R = (dx, dy, h_i + h_j) and d share dx^2 + dy^2;
+//   * the isotropic RPY and image coefficients of F (f and A) and of T (fw and
+//     f1 of C4) are summed before they multiply the source;
+//   * the coupling c (F x d) and the f1 (e x F) term of C3 share their cross
+//     products: with k1 = f1/|R| - c, k2 = f1 e_z - c d_z, k3 = f1 e_z + c d_z
+//       W += (k1 dy Fz - k2 Fy,  k2 Fx - k1 dx Fz,  k1 (dx Fy - dy Fx))
+//       U += (k3 Ty + k1 dy Tz, -k3 Tx - k1 dx Tz, -k1 (dy Tx - dx Ty))
+//     (the UT image uses e' = (-ex, -ey, ez), hence the signs);
+//   * the C3 factors are linear in h/Rz, f2 = a1 h + a0, f3 = b1 h + b0,
+//     f4 = c1 h + c0, so the WF (h_j) and UT (h_i) images share a, b, c;
+//   * (z x e).T serves both the C4 (WT) and the transposed C3 (UT) images;
+//   * t0, r0, rt0 are folded into the polynomial constants.
+// Sources carry b_j in F and T; the caller applies b_i to the sums.
+// ---------------------------------------------------------------------------
+struct WallConst {
+  // UF image (times t0): A = iR (a10 + a11 h1q) + iR3 (a30 + a31 q) + iR5 (a50 + a51 q)
+  float a10, a11, a30, a31, a50, a51;
+  float b10, b11, b30, b31, b50, b51;
+  // C = ez [iR (c1h hh + c11 h1q) + iR3 (c30 + c31 q) + iR5 (c50 + c51 q)]
+  float c1h, c11, c30, c31, c50, c51;
+  // D = ez (d1 hh iR + d5 iR5);  E = e1 q (hh^2 iR + iR3) + iR5 (e50 + e51 q)
+  float d1, d5, e1, e50, e51;
+  // WT image (times r0): f1 = iR3 (w0 + w1 q), f2 = w2 iR3, f4 = -2 f2, f3 = f4 ez
+  float w0, w1, w2;
+  // C3 (times rt0): f1 = g0 iR2; a1 = g1 q iR2, a0 = iR4 (g2 + g3 q);
+  // b1 = g4 ez iR2, b0 = g5 ez iR4; c1 = g6 ez iR2, c0 = g7 ez iR4
+  float g0, g1, g2, g3, g4, g5, g6, g7;
+};
+
+inline WallConst make_wall_const(double t0, double r0, double rt0) {
+  WallConst w;
+  w.a10 = float(-0.75 * t0); w.a11 = float(-1.5 * t0);
+  w.a30 = float(-0.5 * t0);  w.a31 = float(1.5 * t0);
+  w.a50 = float(0.5 * t0);   w.a51 = float(-2.5 * t0);
+  w.b10 = float(-0.75 * t0); w.b11 = float(4.5 * t0);
+  w.b30 = float(1.5 * t0);   w.b31 = float(-7.5 * t0);
+  w.b50 = float(-2.5 * t0);  w.b51 = float(17.5 * t0);
+  w.c1h = float(1.5 * t0);   w.c11 = float(-9.0 * t0);
+  w.c30 = float(-3.0 * t0);  w.c31 = float(15.0 * t0);
+  w.c50 = float(10.0 * t0);  w.c51 = float(-35.0 * t0);
+  w.d1 = float(1.5 * t0);    w.d5 = float(-5.0 * t0);
+  w.e1 = float(-3.0 * t0);   w.e50 = float(-2.0 * t0);  w.e51 = float(15.0 * t0);
+  w.w0 = float(0.5 * r0);    w.w1 = float(-3.0 * r0);   w.w2 = float(-1.5 * r0);
+  w.g0 = float(rt0);         w.g1 = float(12.0 * rt0);
+  w.g2 = float(2.0 * rt0);   w.g3 = float(-20.0 * rt0);
+  w.g4 = float(-6.0 * rt0);  w.g5 = float(10.0 * rt0);
+  w.g6 = float(-2.0 * rt0);  w.g7 = float(2.0 * rt0);
+  return w;
+}
+
+// Adds the UF+UT contribution to u and WT+WF to w for target (xi, yi, hi) and
+// source p = (xj, yj, hj, .), F, T (scaled units, FP32).
+__device__ __forceinline__ void wall_pair_fused(const PairConst<float> &k, const WallConst &K,
+                                                float xi, float yi, float hi, float xj, float yj,
+                                                float hj, float Fx, float Fy, float Fz, float Tx,
+                                                float Ty, float Tz, Vec3<float> &u,
+                                                Vec3<float> &w) {
+  const float dx = xi - xj, dy = yi - yj, dz = hi - hj;
+  const float sxy = fmaf(dx, dx, dy * dy);
+  const float r2 = fmaf(dz, dz, sxy);
+  const float Rz = hi + hj;
+  if (r2 > 0.0f) {
+    const float ir = rsqrtf(r2);
+    float f, G, fw, Gw, c;
+    rpy_coefficients<float, true, true, true>(k, r2, ir, f, G, fw, Gw, c);
+    const float iR = rsqrtf(fmaf(Rz, Rz, sxy));
+    const float ex = dx * iR, ey = dy * iR, ez = Rz * iR;
+    const float iRz = __fdividef(1.0f, Rz);
+    const float hhj = hj * iRz, hhi = hi * iRz;
+    const float q = ez * ez;
+    const float iR2 = iR * iR, iR3 = iR2 * iR, iR5 = iR3 * iR2, iR4 = iR2 * iR2;
+    // ---- translational image C2 (UF), merged with the RPY UF block ----
+    const float h1q = fmaf(-hhj, hhj, hhj) * q;
+    const float A = fmaf(iR, fmaf(K.a11, h1q, K.a10),
+                         fmaf(iR3, fmaf(K.a31, q, K.a30), iR5 * fmaf(K.a51, q, K.a50)));
+    const float B = fmaf(iR, fmaf(K.b11, h1q, K.b10),
+                         fmaf(iR3, fmaf(K.b31, q, K.b30), iR5 * fmaf(K.b51, q, K.b50)));
+    const float C = ez * fmaf(iR, fmaf(K.c1h, hhj, K.c11 * h1q),
+                              fmaf(iR3, fmaf(K.c31, q, K.c30), iR5 * fmaf(K.c51, q, K.c50)));
+    const float D = ez * fmaf(K.d1 * hhj, iR, K.d5 * iR5);
+    const float E = fmaf(K.e1 * q, fmaf(hhj * hhj, iR, iR3), iR5 * fmaf(K.e51, q, K.e50));
+    const float ev = fmaf(ex, Fx, fmaf(ey, Fy, ez * Fz));
+    const float dF = fmaf(dx, Fx, fmaf(dy, Fy, dz * Fz));
+    const float fA = f + A;
+    const float g = G * dF;
+    const float s = fmaf(B, ev, C * Fz);
+    u.x = fmaf(fA, Fx, fmaf(g, dx, fmaf(s, ex, u.x)));
+    u.y = fmaf(fA, Fy, fmaf(g, dy, fmaf(s, ey, u.y)));
+    u.z = fmaf(fA, Fz, fmaf(g, dz, fmaf(s, ez, fmaf(D, ev, fmaf(E, Fz, u.z)))));
+    // ---- rotational image C4 (WT), merged with the RPY WT block ----
+    const float evT = fmaf(ex, Tx, fmaf(ey, Ty, ez * Tz));
+    const float dT = fmaf(dx, Tx, fmaf(dy, Ty, dz * Tz));
+    const float pv = fmaf(ex, Ty, -ey * Tx);  // (z x e).T
+    const float f2w = K.w2 * iR3;
+    const float f4w = -2.0f * f2w;
+    const float fwA = fmaf(iR3, fmaf(K.w1, q, K.w0), fw);
+    const float gw = Gw * dT;
+    const float sT = f2w * evT;
+    const float m = f4w * pv;
+    w.x = fmaf(fwA, Tx, fmaf(gw, dx, fmaf(sT, ex, fmaf(-m, ey, w.x))));
+    w.y = fmaf(fwA, Ty, fmaf(gw, dy, fmaf(sT, ey, fmaf(m, ex, w.y))));
+    w.z = fmaf(fwA, Tz, fmaf(gw, dz, fmaf(sT, ez, (f4w * ez) * evT + w.z)));
+    // ---- couplings: RPY c(F x d), c(T x d) + C3 images (WF with h_j, UT with h_i) ----
+    const float f1 = K.g0 * iR2;
+    const float ga1 = (K.g1 * q) * iR2;
+    const float ga0 = iR4 * fmaf(K.g3, q, K.g2);
+    const float ezR2 = ez * iR2, ezR4 = ez * iR4;
+    const float gb1 = K.g4 * ezR2, gb0 = K.g5 * ezR4;
+    const float gc1 = K.g6 * ezR2, gc0 = K.g7 * ezR4;
+    const float k1 = fmaf(f1, iR, -c);
+    const float p = f1 * ez;
+    const float k2 = fmaf(-c, dz, p);
+    const float k3 = fmaf(c, dz, p);
+    // WF image with h_j
+    const float f2j = fmaf(ga1, hhj, ga0), f3j = fmaf(gb1, hhj, gb0), f4j = fmaf(gc1, hhj, gc0);
+    const float gj = fmaf(f3j, ev, f2j * Fz);
+    const float k1dx = k1 * dx, k1dy = k1 * dy;
+    w.x = fmaf(k1dy, Fz, fmaf(-(k2 + f4j), Fy, fmaf(gj, ey, w.x)));
+    w.y = fmaf(k2 + f4j, Fx, fmaf(-k1dx, Fz, fmaf(-gj, ex, w.y)));
+    w.z = fmaf(k1, fmaf(dx, Fy, -dy * Fx), w.z);
+    // UT image with h_i
+    const float f2i = fmaf(ga1, hhi, ga0), f3i = fmaf(gb1, hhi, gb0), f4i = fmaf(gc1, hhi, gc0);
+    const float mp = pv * f3i;
+    u.x = fmaf(k3 + f4i, Ty, fmaf(k1dy, Tz, fmaf(-mp, ex, u.x)));
+    u.y = fmaf(-(k3 + f4i), Tx, fmaf(-k1dx, Tz, fmaf(-mp, ey, u.y)));
+    u.z = fmaf(-k1, fmaf(dy, Tx, -dx * Ty), fmaf(mp, ez, fmaf(pv, f2i, u.z)));
+  } else {
+    // self pair: RPY self mobilities and the wall self terms B1, B2, B3
+    const float ih = __fdividef(1.0f, hj);
+    const Vec3<float> F3 = {Fx, Fy, Fz}, T3 = {Tx, Ty, Tz};
+    Vec3<float> cu = {0, 0, 0}, cw = {0, 0, 0}, ct = {0, 0, 0}, cf = {0, 0, 0};
+    wall_self_uf<float>(ih, F3, cu);
+    wall_self_wt<float>(ih, T3, cw);
+    wall_self_wf<float>(ih, F3, cf);
+    wall_self_ut<float>(ih, T3, ct);
+    u.x += k.t0 * (Fx + cu.x) + k.rt0 * ct.x;
+    u.y += k.t0 * (Fy + cu.y) + k.rt0 * ct.y;
+    u.z += k.t0 * (Fz + cu.z) + k.rt0 * ct.z;
+    w.x += k.r0 * (Tx + cw.x) + k.rt0 * cf.x;
+    w.y += k.r0 * (Ty + cw.y) + k.rt0 * cf.y;
+    w.z += k.r0 * (Tz + cw.z) + k.rt0 * cf.z;
+  }
+}
+
 }  // namespace lmg

@@ -299,6 +299,7 @@ void Solver<R>::mdot_device(const R *pos, const R *F, const R *T, R *U, R *W) {
   a.nper = nper;
   a.inv_a = (R)(1.0 / a_);
   a.k = make_pair_const<R>(t0_, r0_, rt0_);
+  a.kw = make_wall_const(t0_, r0_, rt0_);
   a.part = part_.ptr;
   a.ticket = tickets_.ptr;
   LMG_CUDA(mdot_launch<R>(s, a, plan, stream()));
