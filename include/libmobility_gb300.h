@@ -159,6 +159,20 @@ lmg_status lmg_langevin_velocities(lmg_solver *h, double dt, double kbt,
 lmg_status lmg_div_m(lmg_solver *h, void *U, size_t nU, void *W, size_t nW,
                      double prefactor);
 
+/* No counterpart in the reference: learned sparse preconditioner for
+ * sqrtMdotW.  kind "none" (default: plain Lanczos as in the reference) or
+ * "mlp": Lanczos then runs on S = P M P^T, where P approximates M^{-1/2}
+ * row by row over each particle's 16 nearest neighbours (an MLP on their
+ * relative positions), and the sample is P^{-1} S^{1/2} dW, whose covariance is
+ * M exactly; P changes the iteration count, not the statistics.  params holds
+ * the network (n_params floats, the layout of libmobility_gb300/precond.py).
+ * Needs precision float; batches of fewer than 17 particles use plain
+ * Lanczos. */
+lmg_status lmg_set_preconditioner(lmg_solver *h, const char *kind, const float *params,
+                                  size_t n_params);
+/* Iterations of the last preconditioner solve P x = S^{1/2} dW. */
+lmg_status lmg_get_preconditioner_solve_iterations(const lmg_solver *h, int *out);
+
 /* Mobility::clean -- MobilityInterface.h:220-223: frees the solver's
  * Lanczos storage and scratch. */
 lmg_status lmg_clean(lmg_solver *h);

@@ -27,6 +27,7 @@ UNITS = [
     ("solver.cu", [], "solver.o"),
     ("probes.cu", [], "probes.o"),
     ("noalloc.cu", [], "noalloc.o"),
+    ("precond.cu", [], "precond.o"),
     ("solver_base.cpp", [], "solver_base.o"),
     ("capi.cpp", [], "capi.o"),
 ]

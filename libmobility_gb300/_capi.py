@@ -48,6 +48,8 @@ SIGNATURES = {
     "lmg_clean": (_I, [_VP]),
     "lmg_synchronize": (_I, [_VP]),
     "lmg_precision_name": (ctypes.c_char_p, [_VP]),
+    "lmg_set_preconditioner": (_I, [_VP, ctypes.c_char_p, _VP, _SZ]),
+    "lmg_get_preconditioner_solve_iterations": (_I, [_VP, ctypes.POINTER(_I)]),
     "lmg_mdot_noalloc_f32": (_I, [_VP, _VP, _VP, _VP, _VP, ctypes.c_int64, ctypes.c_int64, _I,
                                  _D, _D, _I, _VP, ctypes.c_char_p, _SZ]),
 }
@@ -78,6 +80,21 @@ def load():
     lib.lmg_internal_fma_probe.argtypes = [_I, _I, _I, _VP, _VP]
     lib.lmg_internal_fma2_probe.restype = _I
     lib.lmg_internal_fma2_probe.argtypes = [_I, _I, _I, _VP, _VP]
+    _F = ctypes.c_float
+    internal = {
+        "lmg_internal_gemm": [_I, _I, _I, _I, _I, _VP, _I, _VP, _I, _VP, _I, _VP, _I, _F, _VP],
+        "lmg_internal_tanh_backward": [_SZ, _VP, _VP, _VP],
+        "lmg_internal_mse_grad": [_SZ, _VP, _VP, _VP, _F, _VP, _VP],
+        "lmg_internal_colsum": [_I, _I, _VP, _VP, _VP],
+        "lmg_internal_adam": [_SZ, _VP, _VP, _VP, _VP, _F, _F, _F, _F, _I, _VP],
+        "lmg_internal_knn": [_VP, _I, _I, _VP, _VP],
+        "lmg_internal_precond_build": [_VP, _VP, _I, _VP, _F, _F, _VP, _VP],
+        "lmg_internal_precond_apply": [_VP, _VP, _I, _VP, _VP, _I, _VP],
+    }
+    for name, args in internal.items():
+        fn = getattr(lib, name)
+        fn.restype = _I
+        fn.argtypes = args
     _lib = lib
     return lib
 

@@ -155,6 +155,19 @@ lmg_status lmg_div_m(lmg_solver *h, void *U, size_t nU, void *W, size_t nW, doub
   return guarded(h, [&](lmg::SolverBase &m) { m.div_m(U, nU, W, nW, prefactor); });
 }
 
+lmg_status lmg_set_preconditioner(lmg_solver *h, const char *kind, const float *params,
+                                  size_t n_params) {
+  return guarded(h, [&](lmg::SolverBase &m) {
+    m.set_preconditioner(kind ? kind : "none", params, n_params);
+  });
+}
+
+lmg_status lmg_get_preconditioner_solve_iterations(const lmg_solver *h, int *out) {
+  if (!h || !h->impl || !out) return LMG_ERR_INVALID_ARGUMENT;
+  *out = h->impl->last_solve_iterations();
+  return LMG_OK;
+}
+
 lmg_status lmg_clean(lmg_solver *h) {
   return guarded(h, [&](lmg::SolverBase &m) { m.clean(); });
 }

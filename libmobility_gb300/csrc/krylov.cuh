@@ -373,6 +373,82 @@ __global__ void krylov_error_kernel(const R *y, const R *yprev, size_t n, double
   }
 }
 
+// ---------------------------------------------------------------------------
+// BiCGSTAB pieces for solving P x = b with the sparse preconditioner (the
+// last step of the preconditioned square root).  Each reduction writes its
+// FP64 results to mapped host memory (out[0], out[1]).
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void dot2_kernel(const R *a, const R *b, const R *c, const R *d, size_t n,
+                            double *partials, unsigned *ticket, double *out) {
+  double v[2] = {0.0, 0.0};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    v[0] += (double)a[e] * (double)b[e];
+    v[1] += (double)c[e] * (double)d[e];
+  }
+  double tot[2];
+  if (grid_sum<2>(v, partials, ticket, tot)) {
+    out[0] = tot[0];
+    out[1] = tot[1];
+  }
+}
+
+// p = r + beta (p - omega v)
+template <class R>
+__global__ void bicg_p_kernel(R *p, const R *r, const R *v, double beta, double omega, size_t n) {
+  const R b = (R)beta, o = (R)omega;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x)
+    p[e] = r[e] + b * (p[e] - o * v[e]);
+}
+
+// s = r - alpha v ; out[0] = |s|^2
+template <class R>
+__global__ void bicg_s_kernel(R *s, const R *r, const R *v, double alpha, size_t n,
+                              double *partials, unsigned *ticket, double *out) {
+  const R a = (R)alpha;
+  double acc[1] = {0.0};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const R x = r[e] - a * v[e];
+    s[e] = x;
+    acc[0] += (double)x * (double)x;
+  }
+  double tot[1];
+  if (grid_sum<1>(acc, partials, ticket, tot)) out[0] = tot[0];
+}
+
+// x += alpha p + omega s ; r = s - omega t ; out = (|r|^2, rhat . r)
+template <class R>
+__global__ void bicg_xr_kernel(R *x, const R *p, const R *s, const R *t, R *r, const R *rhat,
+                               double alpha, double omega, size_t n, double *partials,
+                               unsigned *ticket, double *out) {
+  const R a = (R)alpha, o = (R)omega;
+  double acc[2] = {0.0, 0.0};
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    x[e] += a * p[e] + o * s[e];
+    const R re = s[e] - o * t[e];
+    r[e] = re;
+    acc[0] += (double)re * (double)re;
+    acc[1] += (double)rhat[e] * (double)re;
+  }
+  double tot[2];
+  if (grid_sum<2>(acc, partials, ticket, tot)) {
+    out[0] = tot[0];
+    out[1] = tot[1];
+  }
+}
+
+// y = c x
+template <class R>
+__global__ void scale_kernel(R *y, const R *x, size_t n, R c) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x)
+    y[e] = c * x[e];
+}
+
 // out += pf * y  (used for both the linear and the angular halves)
 template <class R>
 __global__ void axpy_kernel(R *out, const R *y, size_t n, R pf) {

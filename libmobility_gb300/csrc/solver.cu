@@ -11,11 +11,13 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <type_traits>
 #include <vector>
 
 #include "krylov.cuh"
 #include "launch_count.hpp"
 #include "mdot_launch.cuh"
+#include "precond.cuh"
 #include "solver.hpp"
 
 namespace lmg {
@@ -108,6 +110,7 @@ template <class R> class Solver final : public SolverBase {
                    size_t ndW, int *iterations, double *residual) override;
   void div_m(void *U, size_t nU, void *W, size_t nW, double prefactor) override;
   void clean() override;
+  void set_preconditioner(const std::string &kind, const float *params, size_t n) override;
 
  private:
   // device state
@@ -133,6 +136,12 @@ template <class R> class Solver final : public SolverBase {
   cudaEvent_t ev_iter_[2] = {nullptr, nullptr}, ev_check_ = nullptr, ev_side_ = nullptr;
   // RFD
   DeviceBuffer<R> rfd_noise_, rfd_pos_, rfd_mp_, rfd_mm_;
+  // learned preconditioner
+  bool prec_on_ = false;
+  bool prec_dirty_ = true;
+  DeviceBuffer<float> prec_params_, prec_blocks_;
+  DeviceBuffer<int> prec_nb_;
+  DeviceBuffer<R> pt_, pu_, bx_, br_, brh_, bp_, bv_, bs_, bt_;  // operator and BiCGSTAB vectors
   int num_sms_ = 0;
   bool tickets_zeroed_ = false;
   std::map<long, MdotPlan> plans_;
@@ -151,6 +160,10 @@ template <class R> class Solver final : public SolverBase {
   // M . [F;T] on device buffers: the Lanczos matvec and the RFD probes
   void mdot_device(const R *pos, const R *F, const R *T, R *U, R *W);
   int lanczos(const R *z, R *y, size_t n, double tol, double *residual);
+  bool prec_active() const;
+  void prec_build();
+  void apply_operator(const R *v, R *out);  // M v, or P M P^T v with the preconditioner
+  int solve_p(const R *b, R *x);             // P x = b (BiCGSTAB), returns iterations
 };
 
 template <class R> int Solver<R>::sms() {
@@ -239,6 +252,7 @@ template <class R> void Solver<R>::set_positions(const void *pos, size_t n) {
   std::swap(pos_.ptr, pos_tmp_.ptr);
   std::swap(pos_.count, pos_tmp_.count);
   N_ = N;
+  prec_dirty_ = true;
 }
 
 // Device pointer for a user array: used in place when it is device memory,
@@ -396,7 +410,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
 
   auto issue = [&](int j) {
     R *vj = V + (size_t)j * n;
-    mdot_device(pos_.ptr, vj, ang_ ? vj + n3 : nullptr, w, ang_ ? w + n3 : nullptr);
+    apply_operator(vj, w);
     krylov_alpha_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vj, j > 0 ? vj - n : vj, n, j, rp,
                                                            tk, sc);
     count_launch();
@@ -518,7 +532,21 @@ void Solver<R>::sqrt_mdot_w(void *U, size_t nU, void *W, size_t nW, double prefa
   }
   R *y = y_.ensure(n);
   double res = 0;
+  const bool prec = prec_active();
+  if (prec) prec_build();
   const int it = lanczos(z, y, n, tol_, &res);
+  if (prec) {
+    // y currently holds S^{1/2} z with S = P M P^T; the sample is P^{-1} of it
+    // (translational part by BiCGSTAB, angular part by the scalar factor)
+    R *x = bx_.ensure(n);
+    last_inner_iters_ = solve_p(y, x);
+    if (ang_) {
+      const R sc = (R)std::sqrt(r0_);
+      scale_kernel<R><<<vec_blocks(n3), kRedThreads, 0, stream()>>>(x + n3, y + n3, n3, sc);
+      count_launch();
+    }
+    LMG_CUDA(cudaMemcpyAsync(y, x, n * sizeof(R), cudaMemcpyDeviceToDevice, stream()));
+  }
   if (iterations) *iterations = it;
   if (residual) *residual = res;
   // out += prefactor * y   (MobilityInterface.h:179-187)
@@ -638,6 +666,153 @@ template <class R> void Solver<R>::clean() {
   rot_cs_ = {}; rot_idx_ = {};
   part_.release(); tickets_.release(); tickets_zeroed_ = false; plans_.clear();
   rfd_noise_.release(); rfd_pos_.release(); rfd_mp_.release(); rfd_mm_.release();
+}
+
+template <class R>
+void Solver<R>::set_preconditioner(const std::string &kind, const float *params, size_t n) {
+  if (kind == "none") {
+    prec_on_ = false;
+    return;
+  }
+  if (kind != "mlp")
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] preconditioner must be \"none\" or \"mlp\"");
+  if (!std::is_same<R, float>::value)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] the learned preconditioner needs precision float");
+  if (!params || n != (size_t)kPrecParams)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] preconditioner parameters must hold " +
+                    std::to_string(kPrecParams) + " floats");
+  float *d = prec_params_.ensure(kPrecParams);
+  LMG_CUDA(cudaMemcpy(d, params, kPrecParams * sizeof(float), cudaMemcpyHostToDevice));
+  prec_on_ = true;
+  prec_dirty_ = true;
+}
+
+// The preconditioner needs at least K + 1 particles per batch; smaller
+// systems fall back to plain Lanczos.
+template <class R> bool Solver<R>::prec_active() const {
+  return prec_on_ && std::is_same<R, float>::value && batch_size() >= kPrecK + 1;
+}
+
+template <class R> void Solver<R>::prec_build() {
+  if constexpr (std::is_same<R, float>::value) {
+    if (!prec_dirty_) return;
+    const int N = (int)N_;
+    int *nb = prec_nb_.ensure((size_t)N * kPrecBlocks);
+    float *blocks = prec_blocks_.ensure((size_t)N * kPrecBlocks * 9);
+    LMG_CUDA(knn_launch(pos_.ptr, N, batch_size(), nb, stream()));
+    // targets were trained with t0 = 1: M^{-1/2} scales as t0^{-1/2}
+    LMG_CUDA(precond_build_launch(pos_.ptr, nb, N, prec_params_.ptr, (float)(1.0 / a_),
+                                  (float)(1.0 / std::sqrt(t0_)), blocks, stream()));
+    prec_dirty_ = false;
+  }
+}
+
+template <class R> void Solver<R>::apply_operator(const R *v, R *out) {
+  const size_t n3 = 3 * (size_t)N_;
+  if (!prec_active()) {
+    mdot_device(pos_.ptr, v, ang_ ? v + n3 : nullptr, out, ang_ ? out + n3 : nullptr);
+    return;
+  }
+  if constexpr (std::is_same<R, float>::value) {
+    const int N = (int)N_;
+    const size_t n = ang_ ? 2 * n3 : n3;
+    R *t = pt_.ensure(n);
+    R *u = pu_.ensure(n);
+    const R s = (R)(1.0 / std::sqrt(r0_));  // angular part: scalar r0^{-1/2}
+    LMG_CUDA(cudaMemsetAsync(t, 0, n3 * sizeof(R), stream()));
+    LMG_CUDA(precond_apply_t_launch(prec_blocks_.ptr, prec_nb_.ptr, N, v, t, stream()));
+    if (ang_) {
+      scale_kernel<R><<<vec_blocks(n3), kRedThreads, 0, stream()>>>(t + n3, v + n3, n3, s);
+      count_launch();
+    }
+    mdot_device(pos_.ptr, t, ang_ ? t + n3 : nullptr, u, ang_ ? u + n3 : nullptr);
+    LMG_CUDA(precond_apply_launch(prec_blocks_.ptr, prec_nb_.ptr, N, u, out, stream()));
+    if (ang_) {
+      scale_kernel<R><<<vec_blocks(n3), kRedThreads, 0, stream()>>>(out + n3, u + n3, n3, s);
+      count_launch();
+    }
+  }
+}
+
+// BiCGSTAB (van der Vorst 1992) for P x = b on the translational part,
+// relative residual 1e-7 (the Lanczos tolerance is at least 1e-6 on single
+// precision vectors).  Scalars in FP64 on the host; each reduction is read
+// back through mapped memory.
+template <class R> int Solver<R>::solve_p(const R *b, R *x) {
+  if constexpr (!std::is_same<R, float>::value) {
+    (void)b; (void)x;
+    return 0;
+  } else {
+    const int N = (int)N_;
+    const size_t n = 3 * (size_t)N;
+    cudaStream_t st = stream();
+    const int blocks = vec_blocks(n);
+    ensure_reduction(blocks);
+    unsigned *tk = red_ticket_.ptr;
+    double *rp = red_part_.ptr;
+    double *mir = mirror_.ensure(2 * 256 + 8);
+    double *out = mirror_.device_ptr() + 514;
+    double *hout = mir + 514;
+    R *r = br_.ensure(n), *rh = brh_.ensure(n), *p = bp_.ensure(n), *v = bv_.ensure(n);
+    R *s = bs_.ensure(n), *t = bt_.ensure(n);
+    auto sync = [&]() { LMG_CUDA(cudaStreamSynchronize(st)); };
+    LMG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(R), st));
+    LMG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(R), st));
+    LMG_CUDA(cudaMemsetAsync(v, 0, n * sizeof(R), st));
+    LMG_CUDA(cudaMemcpyAsync(r, b, n * sizeof(R), cudaMemcpyDeviceToDevice, st));
+    LMG_CUDA(cudaMemcpyAsync(rh, b, n * sizeof(R), cudaMemcpyDeviceToDevice, st));
+    dot2_kernel<R><<<blocks, kRedThreads, 0, st>>>(b, b, b, b, n, rp, tk, out);
+    count_launch();
+    sync();
+    const double bnorm2 = hout[0];
+    if (!(bnorm2 > 0)) return 0;
+    const double tol2 = 1e-14 * bnorm2;
+    double rho = 1, alpha = 1, omega = 1, rho1 = bnorm2;
+    const int max_it = 500;
+    for (int it = 1; it <= max_it; it++) {
+      const double beta = (rho1 / rho) * (alpha / omega);
+      bicg_p_kernel<R><<<blocks, kRedThreads, 0, st>>>(p, r, v, it == 1 ? 0.0 : beta,
+                                                       omega, n);
+      count_launch();
+      LMG_CUDA(precond_apply_launch(prec_blocks_.ptr, prec_nb_.ptr, N, p, v, st));
+      dot2_kernel<R><<<blocks, kRedThreads, 0, st>>>(rh, v, rh, v, n, rp, tk, out);
+      count_launch();
+      sync();
+      const double rv = hout[0];
+      if (rv == 0 || std::isnan(rv))
+        throw Error(LMG_ERR_NAN, "[libmobility_gb300] preconditioner solve broke down");
+      alpha = rho1 / rv;
+      bicg_s_kernel<R><<<blocks, kRedThreads, 0, st>>>(s, r, v, alpha, n, rp, tk, out);
+      count_launch();
+      sync();
+      if (hout[0] <= tol2) {  // x += alpha p
+        bicg_xr_kernel<R><<<blocks, kRedThreads, 0, st>>>(x, p, s, s, r, rh, alpha, 0.0, n,
+                                                          rp, tk, out);
+        count_launch();
+        sync();
+        return it;
+      }
+      LMG_CUDA(precond_apply_launch(prec_blocks_.ptr, prec_nb_.ptr, N, s, t, st));
+      dot2_kernel<R><<<blocks, kRedThreads, 0, st>>>(t, s, t, t, n, rp, tk, out);
+      count_launch();
+      sync();
+      omega = hout[0] / hout[1];
+      bicg_xr_kernel<R><<<blocks, kRedThreads, 0, st>>>(x, p, s, t, r, rh, alpha, omega, n, rp,
+                                                        tk, out);
+      count_launch();
+      sync();
+      rho = rho1;
+      rho1 = hout[1];
+      if (hout[0] <= tol2) return it;
+      if (std::isnan(hout[0]))
+        throw Error(LMG_ERR_NAN, "[libmobility_gb300] preconditioner solve broke down");
+    }
+    throw Error(LMG_ERR_NO_CONVERGENCE,
+                "[libmobility_gb300] preconditioner solve did not converge");
+  }
 }
 
 SolverBase *make_solver(Periodicity x, Periodicity y, Periodicity z, int precision) {

@@ -46,6 +46,10 @@ class SolverBase {
   virtual void div_m(void *U, size_t nU, void *W, size_t nW, double prefactor) = 0;
   virtual void clean() = 0;
   virtual const char *precision() const = 0;
+  // learned sparse preconditioner for sqrtMdotW (no counterpart in the
+  // reference): kind "none" or "mlp" with the network's parameters
+  virtual void set_preconditioner(const std::string &kind, const float *params, size_t n) = 0;
+  int last_solve_iterations() const { return last_inner_iters_; }
 
   // Mobility::LangevinVelocities, MobilityInterface.h:191-206
   void langevin(double dt, double kbt, const void *F, size_t nF, const void *T, size_t nT,
@@ -80,6 +84,7 @@ class SolverBase {
   int check_steps_ = 3;      // lanczos::Solver::check_convergence_steps
   int hard_limit_ = 200;     // lanczos::Solver::iterationHardLimit
   lmg_lanczos_callback cb_ = nullptr;
+  int last_inner_iters_ = 0;  // BiCGSTAB iterations of the last preconditioned solve
   void *cb_user_ = nullptr;
   // positions
   int64_t N_ = 0;

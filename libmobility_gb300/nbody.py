@@ -151,6 +151,29 @@ class NBody:
                 return
         self._check(self._lib.lmg_set_stream(self._h, _capi.LMG_OWN_STREAM))
 
+    def setPreconditioner(self, kind="mlp", weights=None):
+        """Learned sparse preconditioner for sqrtMdotW (no counterpart in
+        the reference): "mlp" uses the network shipped in
+        libmobility_gb300/weights (or the .npz given as `weights`); "none"
+        restores plain Lanczos.  The statistics of the samples do not depend
+        on it, only the number of Lanczos iterations."""
+        if kind == "none":
+            self._check(self._lib.lmg_set_preconditioner(self._h, b"none", None, 0))
+            return
+        from . import precond
+        params = np.ascontiguousarray(
+            precond.load_weights(weights) if not isinstance(weights, np.ndarray) else weights,
+            dtype=np.float32)
+        self._prec_params = params
+        self._check(self._lib.lmg_set_preconditioner(self._h, str(kind).encode(),
+                                                     ctypes.c_void_p(params.ctypes.data),
+                                                     params.size))
+
+    def lastPreconditionerSolveIterations(self):
+        it = ctypes.c_int()
+        self._check(self._lib.lmg_get_preconditioner_solve_iterations(self._h, ctypes.byref(it)))
+        return it.value
+
     def setLanczosIterationLimit(self, limit):
         """lanczos::Solver::setIterationHardLimit (LanczosAlgorithm.h:272-274)."""
         self._check(self._lib.lmg_set_lanczos_iteration_limit(self._h, int(limit)))

@@ -1,0 +1,327 @@
+"""Training and loading of the learned sparse preconditioner (see
+csrc/precond.cuh for what P is and why it is sparse).
+
+Training data are made by the method itself: random small particle systems
+(N uniform in 64..512, volume fraction uniform in 0.05..0.3, half of them as
+Gaussian clusters of ~128 particles with sigma = 4a, overlaps at 2a removed);
+for sampled particles the 17-particle neighbourhood mobility (open-boundary RPY,
+t0 = 1, a = 1) is inverted-square-rooted exactly in FP64 (dense eigh) and its
+first block row, rotated into the particle's canonical frame, is the target.
+
+The network is trained on the GPU by this project's own kernels
+(lmg_internal_gemm / _tanh_backward / _mse_grad / _colsum / _adam in
+csrc/precond.cu); PyTorch only provides device memory.
+
+    python -m libmobility_gb300.precond train --systems 20000 --out weights.npz
+"""
+import argparse
+import ctypes
+import json
+import math
+import multiprocessing as mp
+import os
+import time
+from pathlib import Path
+
+import numpy as np
+
+K = 16
+NIN, NH, NOUT = 3 * K, 64, 6 + 9 * K
+WEIGHTS_DIR = Path(__file__).resolve().parent / "weights"
+DEFAULT_WEIGHTS = WEIGHTS_DIR / "precond_open_k16.npz"
+SYM = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+
+
+# ---------------------------------------------------------------------------
+# data
+# ---------------------------------------------------------------------------
+def rpy_uf_blocks(r):
+    """Open-boundary RPY translational blocks M_ij(r) for r = r_i - r_j in
+    units of a, with t0 = 1 (solvers/NBody/extra/hydrodynamicKernels.cuh:41-57,
+    143-150).  r: (..., 3) -> (..., 3, 3)."""
+    d = np.linalg.norm(r, axis=-1)
+    ds = np.maximum(d, 1e-12)
+    far = d >= 2.0
+    f = np.where(far, 0.75 / ds + 0.5 / ds ** 3, 1.0 - 0.28125 * d)
+    g = np.where(far, (0.75 - 1.5 / ds ** 2) / ds ** 3, np.where(d > 0, 0.09375 / ds, 0.0))
+    eye = np.eye(3)
+    return f[..., None, None] * eye + g[..., None, None] * r[..., :, None] * r[..., None, :]
+
+
+def random_system(rng, n, phi, clustered, sigma=4.0):
+    """Positions (units of a) without overlaps below 2a."""
+    from scipy.spatial import cKDTree
+    L = (n * 4 * math.pi / 3 / phi) ** (1 / 3)
+    if clustered:
+        ncl = max(1, n // 128)
+        centres = rng.uniform(0, L, (ncl, 3))
+        lab = rng.integers(0, ncl, n)
+        p = centres[lab] + rng.normal(0, sigma, (n, 3))
+    else:
+        p = rng.uniform(0, L, (n, 3))
+    for _ in range(500):
+        pairs = cKDTree(p).query_pairs(2.0, output_type="ndarray")
+        if len(pairs) == 0:
+            break
+        bad = np.unique(pairs[:, 1])
+        if clustered:
+            p[bad] = centres[lab[bad]] + rng.normal(0, sigma, (len(bad), 3))
+        else:
+            p[bad] = rng.uniform(0, L, (len(bad), 3))
+    return p
+
+
+def canonical_frames(rel):
+    """rel: (B, K, 3) neighbours sorted by distance -> E (B, 3, 3), rows = axes
+    (x to the nearest neighbour, y to the first non-collinear one)."""
+    B = rel.shape[0]
+    ex = rel[:, 0] / np.linalg.norm(rel[:, 0], axis=1, keepdims=True)
+    ey = np.zeros_like(ex)
+    done = np.zeros(B, bool)
+    for n in range(1, K):
+        a = rel[:, n] - ex * np.sum(rel[:, n] * ex, axis=1, keepdims=True)
+        nn = np.sum(a * a, axis=1)
+        take = (~done) & (nn > 1e-12)
+        ey[take] = a[take] / np.sqrt(nn[take])[:, None]
+        done |= take
+    ey[~done] = [0.0, 1.0, 0.0]
+    ez = np.cross(ex, ey)
+    return np.stack([ex, ey, ez], axis=1)
+
+
+def samples_from_system(p, ids):
+    """Features X (B, 48) and targets Y (B, 150) for particles `ids` of p."""
+    from scipy.spatial import cKDTree
+    _, nb = cKDTree(p).query(p[ids], K + 1)
+    rel = p[nb[:, 1:]] - p[ids][:, None, :]
+    E = canonical_frames(rel)
+    X = np.einsum("bnk,bck->bnc", rel, E).reshape(len(ids), -1)
+    P = p[nb]                                                   # B, 17, 3
+    blocks = rpy_uf_blocks(P[:, :, None, :] - P[:, None, :, :])  # B,17,17,3,3
+    Mp = blocks.transpose(0, 1, 3, 2, 4).reshape(len(ids), 3 * (K + 1), 3 * (K + 1))
+    lam, Q = np.linalg.eigh(Mp)
+    row = np.einsum("bij,bj,bkj->bik", Q[:, :3, :], 1.0 / np.sqrt(lam), Q)  # B,3,51
+    rb = row.reshape(len(ids), 3, K + 1, 3).transpose(0, 2, 1, 3)         # B,17,3,3
+    rc = np.einsum("bij,bnjk,blk->bnil", E, rb, E)                         # canonical frame
+    Y = np.concatenate([np.stack([rc[:, 0, i, j] for i, j in SYM], 1),
+                        rc[:, 1:].reshape(len(ids), -1)], 1)
+    return X.astype(np.float32), Y.astype(np.float32)
+
+
+def _make_chunk(args):
+    seed, nsys, per_sys = args
+    rng = np.random.default_rng(seed)
+    Xs, Ys = [], []
+    for _ in range(nsys):
+        n = int(rng.integers(64, 513))
+        phi = float(rng.uniform(0.05, 0.3))
+        p = random_system(rng, n, phi, rng.random() < 0.5)
+        ids = rng.choice(n, min(n, per_sys), replace=False)
+        X, Y = samples_from_system(p, ids)
+        Xs.append(X)
+        Ys.append(Y)
+    return np.concatenate(Xs), np.concatenate(Ys)
+
+
+def make_dataset(systems, per_sys=32, seed=0, workers=None):
+    workers = workers or max(1, (os.cpu_count() or 1))
+    chunk = max(1, systems // (4 * workers))
+    jobs = []
+    s = 0
+    while s < systems:
+        jobs.append((seed * 1000003 + len(jobs), min(chunk, systems - s), per_sys))
+        s += chunk
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        parts = pool.map(_make_chunk, jobs)
+    return np.concatenate([a for a, _ in parts]), np.concatenate([b for _, b in parts])
+
+
+# ---------------------------------------------------------------------------
+# parameters
+# ---------------------------------------------------------------------------
+LAYOUT = [("W1", (NIN, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)),
+          ("W3", (NH, NOUT)), ("b3", (NOUT,)), ("xmean", (NIN,)), ("xstd", (NIN,)),
+          ("ymean", (NOUT,)), ("ystd", (NOUT,))]
+NTRAIN = NIN * NH + NH + NH * NH + NH + NH * NOUT + NOUT  # trainable prefix
+
+
+def flat_params(d):
+    return np.concatenate([np.asarray(d[k], np.float32).ravel() for k, _ in LAYOUT])
+
+
+def load_weights(path=None):
+    """Flat FP32 parameter vector in the layout of csrc/precond.cuh."""
+    path = Path(path) if path else DEFAULT_WEIGHTS
+    if not path.exists():
+        raise FileNotFoundError(f"preconditioner weights {path} not found")
+    z = np.load(path)
+    return flat_params(z)
+
+
+# ---------------------------------------------------------------------------
+# training on the GPU with this project's kernels
+# ---------------------------------------------------------------------------
+class GpuMLP:
+    def __init__(self, lib, torch, params, stream):
+        self.lib, self.torch, self.s = lib, torch, stream
+        self.p = torch.tensor(params, device="cuda")
+        self.g = torch.zeros(NTRAIN, device="cuda")
+        self.m = torch.zeros(NTRAIN, device="cuda")
+        self.v = torch.zeros(NTRAIN, device="cuda")
+        self.loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+        off = 0
+        self.view = {}
+        self.gview = {}
+        for k, shp in LAYOUT:
+            n = int(np.prod(shp))
+            self.view[k] = self.p[off:off + n]
+            if off < NTRAIN:
+                self.gview[k] = self.g[off:off + n]
+            off += n
+
+    def _ptr(self, t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    def gemm(self, ta, tb, M, N, K_, A, lda, B, ldb, C, ldc, bias=None, act=0, beta=0.0):
+        rc = self.lib.lmg_internal_gemm(int(ta), int(tb), M, N, K_, self._ptr(A), lda,
+                                        self._ptr(B), ldb, self._ptr(C), ldc,
+                                        self._ptr(bias) if bias is not None else None, act,
+                                        ctypes.c_float(beta), self.s)
+        assert rc == 0, rc
+
+    def forward(self, X, H1, H2, Yp):
+        B = X.shape[0]
+        v = self.view
+        self.gemm(0, 0, B, NH, NIN, X, NIN, v["W1"], NH, H1, NH, v["b1"], 1)
+        self.gemm(0, 0, B, NH, NH, H1, NH, v["W2"], NH, H2, NH, v["b2"], 1)
+        self.gemm(0, 0, B, NOUT, NH, H2, NH, v["W3"], NOUT, Yp, NOUT, v["b3"], 0)
+
+    def backward(self, X, H1, H2, Yp, T, dY, dH2, dH1):
+        B = X.shape[0]
+        v, g, lib = self.view, self.gview, self.lib
+        scale = ctypes.c_float(2.0 / (B * NOUT))
+        assert lib.lmg_internal_mse_grad(ctypes.c_size_t(B * NOUT), self._ptr(Yp), self._ptr(T),
+                                         self._ptr(dY), scale, self._ptr(self.loss), self.s) == 0
+        self.gemm(1, 0, NH, NOUT, B, H2, NH, dY, NOUT, g["W3"], NOUT)         # dW3 = H2^T dY
+        assert lib.lmg_internal_colsum(B, NOUT, self._ptr(dY), self._ptr(g["b3"]), self.s) == 0
+        self.gemm(0, 1, B, NH, NOUT, dY, NOUT, v["W3"], NOUT, dH2, NH)       # dH2 = dY W3^T
+        assert lib.lmg_internal_tanh_backward(ctypes.c_size_t(B * NH), self._ptr(H2),
+                                              self._ptr(dH2), self.s) == 0
+        self.gemm(1, 0, NH, NH, B, H1, NH, dH2, NH, g["W2"], NH)             # dW2 = H1^T dH2
+        assert lib.lmg_internal_colsum(B, NH, self._ptr(dH2), self._ptr(g["b2"]), self.s) == 0
+        self.gemm(0, 1, B, NH, NH, dH2, NH, v["W2"], NH, dH1, NH)            # dH1 = dH2 W2^T
+        assert lib.lmg_internal_tanh_backward(ctypes.c_size_t(B * NH), self._ptr(H1),
+                                              self._ptr(dH1), self.s) == 0
+        self.gemm(1, 0, NIN, NH, B, X, NIN, dH1, NH, g["W1"], NH)            # dW1 = X^T dH1
+        assert lib.lmg_internal_colsum(B, NH, self._ptr(dH1), self._ptr(g["b1"]), self.s) == 0
+
+    def adam(self, lr, step):
+        assert self.lib.lmg_internal_adam(ctypes.c_size_t(NTRAIN), self._ptr(self.p),
+                                          self._ptr(self.g), self._ptr(self.m), self._ptr(self.v),
+                                          ctypes.c_float(lr), ctypes.c_float(0.9),
+                                          ctypes.c_float(0.999), ctypes.c_float(1e-8), step,
+                                          self.s) == 0
+
+
+def init_params(X, Y, seed=0):
+    rng = np.random.default_rng(seed)
+    d = {}
+    d["W1"] = rng.normal(0, 1 / math.sqrt(NIN), (NIN, NH))
+    d["b1"] = np.zeros(NH)
+    d["W2"] = rng.normal(0, 1 / math.sqrt(NH), (NH, NH))
+    d["b2"] = np.zeros(NH)
+    d["W3"] = rng.normal(0, 1 / math.sqrt(NH), (NH, NOUT))
+    d["b3"] = np.zeros(NOUT)
+    d["xmean"], d["xstd"] = X.mean(0), X.std(0) + 1e-6
+    d["ymean"], d["ystd"] = Y.mean(0), Y.std(0) + 1e-6
+    return d
+
+
+def train(X, Y, epochs=60, batch=4096, lr=2e-3, seed=0, log=print, val_frac=0.05):
+    import torch
+    from . import _capi
+    lib = _capi.load()
+    d = init_params(X, Y, seed)
+    params = flat_params(d)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    net = GpuMLP(lib, torch, params, stream)
+    xm, xs = d["xmean"].astype(np.float32), d["xstd"].astype(np.float32)
+    ym, ys = d["ymean"].astype(np.float32), d["ystd"].astype(np.float32)
+    Xn = torch.tensor((X - xm) / xs, device="cuda")
+    Yn = torch.tensor((Y - ym) / ys, device="cuda")
+    n = Xn.shape[0]
+    nval = max(1, int(val_frac * n))
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    perm = torch.randperm(n, generator=g).cuda()
+    Xv, Yv = Xn[perm[:nval]], Yn[perm[:nval]]
+    Xt, Yt = Xn[perm[nval:]], Yn[perm[nval:]]
+    ntr = Xt.shape[0]
+    H1 = torch.empty(batch, NH, device="cuda")
+    H2 = torch.empty_like(H1)
+    Yp = torch.empty(batch, NOUT, device="cuda")
+    dY = torch.empty_like(Yp)
+    dH1 = torch.empty_like(H1)
+    dH2 = torch.empty_like(H1)
+    step = 0
+    hist = []
+    t0 = time.time()
+    for ep in range(epochs):
+        order = torch.randperm(ntr, generator=g).cuda()
+        cur_lr = lr * (0.5 * (1 + math.cos(math.pi * ep / epochs)))
+        net.loss.zero_()
+        for b0 in range(0, ntr - batch + 1, batch):
+            idx = order[b0:b0 + batch]
+            xb = Xt[idx].contiguous()
+            tb = Yt[idx].contiguous()
+            net.forward(xb, H1, H2, Yp)
+            net.backward(xb, H1, H2, Yp, tb, dY, dH2, dH1)
+            step += 1
+            net.adam(cur_lr, step)
+        train_mse = float(net.loss.item()) / ((ntr // batch) * batch * NOUT)
+        val = evaluate(net, Xv, Yv, batch, torch)
+        hist.append((ep, train_mse, val))
+        if ep % 5 == 0 or ep == epochs - 1:
+            log(f"epoch {ep:3d} train mse {train_mse:.4f} val mse {val:.4f} ({time.time()-t0:.1f}s)")
+    out = {k: net.view[k].detach().cpu().numpy().reshape(shp) for k, shp in LAYOUT}
+    out["xmean"], out["xstd"], out["ymean"], out["ystd"] = xm, xs, ym, ys
+    return out, hist
+
+
+def evaluate(net, Xv, Yv, batch, torch):
+    tot = 0.0
+    for b0 in range(0, Xv.shape[0], batch):
+        xb = Xv[b0:b0 + batch].contiguous()
+        B = xb.shape[0]
+        H1 = torch.empty(B, NH, device="cuda")
+        H2 = torch.empty_like(H1)
+        Yp = torch.empty(B, NOUT, device="cuda")
+        net.forward(xb, H1, H2, Yp)
+        tot += float(((Yp - Yv[b0:b0 + B]) ** 2).sum())
+    return tot / (Xv.shape[0] * NOUT)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    sub = ap.add_subparsers(dest="cmd")
+    t = sub.add_parser("train")
+    t.add_argument("--systems", type=int, default=20000)
+    t.add_argument("--per-system", type=int, default=32)
+    t.add_argument("--epochs", type=int, default=60)
+    t.add_argument("--out", default=str(DEFAULT_WEIGHTS))
+    t.add_argument("--seed", type=int, default=0)
+    a = ap.parse_args()
+    if a.cmd == "train":
+        t0 = time.time()
+        X, Y = make_dataset(a.systems, a.per_system, a.seed)
+        print(f"dataset {X.shape} {Y.shape} in {time.time()-t0:.1f}s", flush=True)
+        w, hist = train(X, Y, epochs=a.epochs, seed=a.seed)
+        Path(a.out).parent.mkdir(parents=True, exist_ok=True)
+        np.savez(a.out, **w, history=np.array(hist),
+                 info=np.array(json.dumps({"systems": a.systems, "per_system": a.per_system,
+                                           "epochs": a.epochs, "samples": int(X.shape[0])})))
+        print("saved", a.out)
+
+
+if __name__ == "__main__":
+    main()

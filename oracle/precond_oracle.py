@@ -1,0 +1,103 @@
+"""NumPy restatement of the learned preconditioner's pieces, for tests
+(TEST INFRASTRUCTURE ONLY; the product never imports it).
+
+Written independently of libmobility_gb300/precond.py: neighbour lists from
+scipy's k-d tree, the canonical frame, the MLP forward and backward passes
+(48 -> 64 tanh -> 64 tanh -> 150) and the sparse P blocks in the lab frame.
+"""
+import numpy as np
+
+K = 16
+NIN, NH, NOUT = 48, 64, 150
+SHAPES = [("W1", (NIN, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)),
+          ("W3", (NH, NOUT)), ("b3", (NOUT,)), ("xmean", (NIN,)), ("xstd", (NIN,)),
+          ("ymean", (NOUT,)), ("ystd", (NOUT,))]
+
+
+def unpack(flat):
+    out, o = {}, 0
+    for k, shp in SHAPES:
+        n = int(np.prod(shp))
+        out[k] = np.asarray(flat[o:o + n], np.float64).reshape(shp)
+        o += n
+    return out
+
+
+def pack(d):
+    return np.concatenate([np.asarray(d[k], np.float32).ravel() for k, _ in SHAPES])
+
+
+def neighbours(pos, k=K):
+    from scipy.spatial import cKDTree
+    d, nb = cKDTree(pos).query(pos, k + 1)
+    return nb, d
+
+
+def frame(rel):
+    """Rows: x to rel[0], y to the first rel[n] not collinear with it."""
+    x = rel[0] / np.linalg.norm(rel[0])
+    y = np.array([0.0, 1.0, 0.0])
+    for n in range(1, len(rel)):
+        a = rel[n] - x * (rel[n] @ x)
+        if a @ a > 1e-12:
+            y = a / np.linalg.norm(a)
+            break
+    return np.stack([x, y, np.cross(x, y)])
+
+
+def forward(d, X):
+    """Returns (H1, H2, Ynorm) for normalised inputs X (B, 48)."""
+    H1 = np.tanh(X @ d["W1"] + d["b1"])
+    H2 = np.tanh(H1 @ d["W2"] + d["b2"])
+    return H1, H2, H2 @ d["W3"] + d["b3"]
+
+
+def backward(d, X, H1, H2, Y, T):
+    """Gradients of mean((Y - T)^2) with respect to W1..b3."""
+    B = X.shape[0]
+    dY = 2.0 * (Y - T) / (B * Y.shape[1])
+    g = {"W3": H2.T @ dY, "b3": dY.sum(0)}
+    dH2 = (dY @ d["W3"].T) * (1 - H2 ** 2)
+    g["W2"], g["b2"] = H1.T @ dH2, dH2.sum(0)
+    dH1 = (dH2 @ d["W2"].T) * (1 - H1 ** 2)
+    g["W1"], g["b1"] = X.T @ dH1, dH1.sum(0)
+    return g
+
+
+def p_blocks(pos, flat, a=1.0, scale=1.0):
+    """Lab-frame blocks (N, 17, 3, 3) and neighbour lists (N, 17)."""
+    d = unpack(flat)
+    nb, _ = neighbours(pos)
+    N = pos.shape[0]
+    out = np.zeros((N, K + 1, 3, 3))
+    for i in range(N):
+        rel = (pos[nb[i, 1:]] - pos[i]) / a
+        E = frame(rel)
+        x = ((rel @ E.T).ravel() - d["xmean"]) / d["xstd"]
+        _, _, y = forward(d, x[None, :])
+        y = y[0] * d["ystd"] + d["ymean"]
+        b = [np.array([[y[0], y[1], y[2]], [y[1], y[3], y[4]], [y[2], y[4], y[5]]])]
+        b += list(y[6:].reshape(K, 3, 3))
+        for n in range(K + 1):
+            out[i, n] = E.T @ b[n] @ E * scale
+    return out, nb
+
+
+def dense_p(blocks, nb):
+    N = blocks.shape[0]
+    P = np.zeros((3 * N, 3 * N))
+    for i in range(N):
+        for n in range(K + 1):
+            j = nb[i, n]
+            P[3 * i:3 * i + 3, 3 * j:3 * j + 3] += blocks[i, n]
+    return P
+
+
+def identity_params():
+    """A network whose output is the identity self block and zero neighbour
+    blocks for every input (all weights zero, output mean = identity)."""
+    d = {k: np.zeros(shp) for k, shp in SHAPES}
+    d["xstd"][:] = 1.0
+    d["ystd"][:] = 1.0
+    d["ymean"][[0, 3, 5]] = 1.0
+    return pack(d)
