@@ -123,8 +123,11 @@ def _make_chunk(args):
     return np.concatenate(Xs), np.concatenate(Ys)
 
 
-def make_dataset(systems, per_sys=32, seed=0, workers=None):
+def make_dataset(systems, per_sys=32, seed=0, workers=None, log=None):
     workers = workers or max(1, (os.cpu_count() or 1))
+    # one BLAS thread per worker: the pool already uses every core
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
     chunk = max(1, systems // (4 * workers))
     jobs = []
     s = 0
@@ -132,8 +135,13 @@ def make_dataset(systems, per_sys=32, seed=0, workers=None):
         jobs.append((seed * 1000003 + len(jobs), min(chunk, systems - s), per_sys))
         s += chunk
     ctx = mp.get_context("spawn")
+    parts = []
+    t0 = time.time()
     with ctx.Pool(workers) as pool:
-        parts = pool.map(_make_chunk, jobs)
+        for k, part in enumerate(pool.imap_unordered(_make_chunk, jobs)):
+            parts.append(part)
+            if log and (k + 1) % max(1, len(jobs) // 10) == 0:
+                log(f"  dataset {k + 1}/{len(jobs)} chunks, {time.time() - t0:.1f}s")
     return np.concatenate([a for a, _ in parts]), np.concatenate([b for _, b in parts])
 
 
@@ -313,7 +321,8 @@ def main():
     a = ap.parse_args()
     if a.cmd == "train":
         t0 = time.time()
-        X, Y = make_dataset(a.systems, a.per_system, a.seed)
+        X, Y = make_dataset(a.systems, a.per_system, a.seed,
+                            log=lambda m: print(m, flush=True))
         print(f"dataset {X.shape} {Y.shape} in {time.time()-t0:.1f}s", flush=True)
         w, hist = train(X, Y, epochs=a.epochs, seed=a.seed)
         Path(a.out).parent.mkdir(parents=True, exist_ok=True)
