@@ -213,6 +213,50 @@ def mdot_kernel_time(torch, s, dF, dT, reps=20):
         return e0.elapsed_time(e1) * 1e-3 / reps, f"back-to-back calls ({exc.__class__.__name__})"
 
 
+def sqrtmdotw_comparison(torch, steps, warmup, rank, N=65536):
+    """Plain vs learned-preconditioned sqrtMdotW on the clustered workload:
+    N = 65536 particles in 512 Gaussian clusters (sigma = 4a, hard-sphere
+    rejection at 2a), volume fraction 0.2, open boundary, tolerance 1e-6.
+    Positions are set again before every solve, so the preconditioner (kNN +
+    network) is rebuilt each time, as in a time-stepping run."""
+    from libmobility_gb300 import NBody
+    from libmobility_gb300.precond import random_system
+    rng = np.random.default_rng(2025 + rank)
+    t0 = time.perf_counter()
+    pos = random_system(rng, N, 0.2, True)
+    gen_s = time.perf_counter() - t0
+    dpos = torch.tensor(pos, dtype=torch.float32, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(77 + rank)
+    dWs = [torch.randn(3 * N, generator=g, device="cuda") for _ in range(steps + warmup)]
+    out = {"workload": "open RPY, N=65536, 512 Gaussian clusters sigma=4a, hard-sphere "
+                       "rejection at 2a, phi=0.2, tolerance 1e-6",
+           "generation_s": gen_s}
+    for kind in ("none", "mlp"):
+        s = NBody("open", "open", "open", precision="float")
+        s.setParameters()
+        s.initialize(viscosity=1 / (6 * math.pi), hydrodynamicRadius=1.0, tolerance=1e-6,
+                     seed=3 + rank)
+        s.setPreconditioner(kind)
+        its, inner, times = [], [], []
+        for k, dW in enumerate(dWs):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.setPositions(dpos)
+            _, _, it, _ = s.sqrtMdotW_noise(dW)
+            torch.cuda.synchronize()
+            if k >= warmup:
+                times.append(time.perf_counter() - t0)
+                its.append(it)
+                inner.append(s.lastPreconditionerSolveIterations() if kind == "mlp" else 0)
+        t = sum(times) / len(times)
+        out[kind] = {"solves_per_s": 1.0 / t, "ms_per_solve": t * 1e3,
+                     "lanczos_iterations": sum(its) / len(its)}
+        if kind == "mlp":
+            out[kind]["p_solve_iterations"] = sum(inner) / len(inner)
+    out["speedup_learned_vs_plain"] = out["mlp"]["solves_per_s"] / out["none"]["solves_per_s"]
+    return out
+
+
 def cpu_baseline(w, pos, F, T, seconds=8.0):
     """FP64 C oracle (all host threads) on a bounded sample of the workload:
     the first R target rows against every source."""
@@ -362,6 +406,10 @@ def run_ours(args, w, ws, rank, local):
     d2h = 2 * 4 * 3 * N * (2 if w["ang"] else 1)
     e2e_value = pairs * (1 + (it_e2e + 1)) * ws / t_e2e
 
+    cmp = None
+    if not args.skip_precond:
+        cmp = sqrtmdotw_comparison(torch, max(2, args.steps), 2, rank)
+
     if rank != 0:
         return
     cpu = cpu_baseline(w, pos, F, T)
@@ -375,6 +423,7 @@ def run_ours(args, w, ws, rank, local):
                    "parallelism": f"replicas x{ws}"},
         "sqrtMdotW": {"solves_per_s": 1.0 / t_sqrt, "lanczos_iterations": it_mean,
                       "preconditioner": "none (plain Lanczos)"},
+        "sqrtMdotW_learned_vs_plain": cmp,
         "mdot_pair_interactions_per_s": pairs / t_mdot,
         "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
@@ -398,6 +447,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="wall16k", choices=sorted(WORKLOADS))
+    ap.add_argument("--skip-precond", action="store_true",
+                    help="skip the plain vs learned-preconditioner sqrtMdotW comparison")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     ws, rank, local = dist_setup()

@@ -48,26 +48,62 @@ def rpy_uf_blocks(r):
     return f[..., None, None] * eye + g[..., None, None] * r[..., :, None] * r[..., None, :]
 
 
-def random_system(rng, n, phi, clustered, sigma=4.0):
-    """Positions (units of a) without overlaps below 2a."""
+def random_system(rng, n, phi, clustered, sigma=4.0, max_rounds=5000):
+    """Positions (units of a) with no pair closer than 2a: points are drawn
+    (uniform in a cube of volume fraction phi, or from Gaussian clusters of
+    ~128 particles with width sigma), and every point that overlaps an
+    accepted one is redrawn from its own distribution until it fits -- hard-
+    sphere rejection, done in rounds over all rejected points at once.  The
+    few points still rejected after 50 rounds are drawn 2 % wider every 50
+    rounds (the core of a 128-particle cluster of width 4a is too dense for
+    the last ones)."""
     from scipy.spatial import cKDTree
     L = (n * 4 * math.pi / 3 / phi) ** (1 / 3)
+    widen = [1.0]  # the last few points of a dense cluster rarely fit at width sigma
     if clustered:
         ncl = max(1, n // 128)
         centres = rng.uniform(0, L, (ncl, 3))
         lab = rng.integers(0, ncl, n)
-        p = centres[lab] + rng.normal(0, sigma, (n, 3))
+
+        def draw(idx):
+            return centres[lab[idx]] + rng.normal(0, sigma * widen[0], (len(idx), 3))
     else:
-        p = rng.uniform(0, L, (n, 3))
-    for _ in range(500):
-        pairs = cKDTree(p).query_pairs(2.0, output_type="ndarray")
-        if len(pairs) == 0:
+        def draw(idx):
+            return rng.uniform(0, L, (len(idx), 3))
+    p = draw(np.arange(n))
+    # first pass: drop one point of every overlapping pair
+    pairs = cKDTree(p).query_pairs(2.0, output_type="ndarray")
+    pending = np.unique(pairs[:, 1]) if len(pairs) else np.zeros(0, int)
+    accepted = np.ones(n, bool)
+    accepted[pending] = False
+    tree = None
+    recent = np.zeros((0, 3))  # accepted since the tree was built
+    for rnd in range(max_rounds):
+        if len(pending) == 0:
             break
-        bad = np.unique(pairs[:, 1])
-        if clustered:
-            p[bad] = centres[lab[bad]] + rng.normal(0, sigma, (len(bad), 3))
-        else:
-            p[bad] = rng.uniform(0, L, (len(bad), 3))
+        if rnd and rnd % 50 == 0:
+            widen[0] *= 1.02
+        if tree is None or len(recent) > 2048:
+            tree = cKDTree(p[accepted])
+            recent = np.zeros((0, 3))
+        cand = draw(pending)
+        hit = tree.query_ball_point(cand, 2.0, return_length=True, workers=-1) > 0
+        if len(recent):
+            hit |= cKDTree(recent).query_ball_point(cand, 2.0, return_length=True) > 0
+        ok = ~hit
+        # among the candidates that fit, keep one of each overlapping pair
+        if ok.sum() > 1:
+            sub = np.flatnonzero(ok)
+            cp = cKDTree(cand[sub]).query_pairs(2.0, output_type="ndarray")
+            if len(cp):
+                ok[sub[np.unique(cp[:, 1])]] = False
+        idx = pending[ok]
+        p[idx] = cand[ok]
+        accepted[idx] = True
+        recent = np.concatenate([recent, cand[ok]])
+        pending = pending[~ok]
+    if len(pending):
+        raise RuntimeError(f"could not place {len(pending)} particles without overlap")
     return p
 
 
