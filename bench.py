@@ -98,6 +98,13 @@ def max_over_ranks(x, ws):
     return float(t.item())
 
 
+def aggregate_rate(units_per_rank, seconds, ws):
+    """Whole-job rate of a replicated run: every rank processed
+    `units_per_rank` in its own time; the job rate is all ranks' units over
+    the slowest rank's time (max over ranks)."""
+    return units_per_rank * ws / max_over_ranks(seconds, ws)
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during a region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -354,11 +361,12 @@ def run_ours(args, w, ws, rank, local):
         barrier(ws)
     launches = lib.lmg_internal_launch_count() - n0
     clocks = clk.summary()
-    t_step = max_over_ranks(sum(times) / len(times), ws)
     pairs = N * N
     it_mean = sum(iters) / len(iters)
     pairs_per_step = pairs * (1 + (it_mean + 1))  # Mdot + (iterations+1) matvecs
-    value = pairs_per_step * ws / t_step
+    t_local = sum(times) / len(times)
+    value = aggregate_rate(pairs_per_step, t_local, ws)
+    t_step = max_over_ranks(t_local, ws)
 
     # --- kernel-level figures: Mdot alone ---
     t_mdot, kernel_timing = mdot_kernel_time(torch, s, dF, dT)

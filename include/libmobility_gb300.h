@@ -78,6 +78,15 @@ lmg_status lmg_create(const char *periodicityX, const char *periodicityY,
                       const char *periodicityZ, int precision, lmg_solver **out);
 const char *lmg_create_error(void);
 
+/* SelfMobility(Configuration) -- solvers/SelfMobility/mobility.h:31-36: the
+ * same handle API for the solver without hydrodynamic interactions (mobility
+ * 1/(6 pi eta a) and 1/(8 pi eta a^3) times the identity, noise drawn on the
+ * host exactly as the reference draws it).  All three periodicities must be
+ * "open".  Its setParameters takes no effect (mobility.h:54). */
+lmg_status lmg_create_self_mobility(const char *periodicityX, const char *periodicityY,
+                                    const char *periodicityZ, int precision,
+                                    lmg_solver **out);
+
 /* Frees the handle and everything it owns. */
 lmg_status lmg_destroy(lmg_solver *h);
 

@@ -12,7 +12,7 @@ mobility solver with the interface of libMobility's NBody.
 The numeric work runs in the in-tree native library liblmg_gb300.so (C ABI in
 include/libmobility_gb300.h); importing NBody fails if it is not built.
 """
-from .nbody import NBody
+from .nbody import NBody, SelfMobility
 
-__all__ = ["NBody"]
+__all__ = ["NBody", "SelfMobility"]
 __version__ = "1.1"

@@ -30,6 +30,7 @@ UNITS = [
     ("precond.cu", [], "precond.o"),
     ("solver_base.cpp", [], "solver_base.o"),
     ("capi.cpp", [], "capi.o"),
+    ("self_mobility.cpp", [], "self_mobility.o"),
 ]
 
 

@@ -31,6 +31,8 @@ SIGNATURES = {
     "lmg_create": (_I, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _I,
                         ctypes.POINTER(_VP)]),
     "lmg_create_error": (ctypes.c_char_p, []),
+    "lmg_create_self_mobility": (_I, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _I,
+                                      ctypes.POINTER(_VP)]),
     "lmg_destroy": (_I, [_VP]),
     "lmg_set_stream": (_I, [_VP, _VP]),
     "lmg_set_lanczos_iteration_limit": (_I, [_VP, _I]),

@@ -66,6 +66,29 @@ lmg_status lmg_create(const char *px, const char *py, const char *pz, int precis
   }
 }
 
+lmg_status lmg_create_self_mobility(const char *px, const char *py, const char *pz,
+                                    int precision, lmg_solver **out) {
+  if (!out) return LMG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  try {
+    if (!px || !py || !pz) throw lmg::Error(LMG_ERR_INVALID_ARGUMENT, "[libMobility] Invalid periodicity");
+    auto x = lmg::parse_periodicity(px);
+    auto y = lmg::parse_periodicity(py);
+    auto z = lmg::parse_periodicity(pz);
+    auto *h = new lmg_solver;
+    h->impl.reset(lmg::make_self_mobility(x, y, z, precision));
+    *out = h;
+    g_create_error.clear();
+    return LMG_OK;
+  } catch (const lmg::Error &e) {
+    g_create_error = e.what();
+    return e.code;
+  } catch (const std::exception &e) {
+    g_create_error = e.what();
+    return LMG_ERR_INTERNAL;
+  }
+}
+
 lmg_status lmg_destroy(lmg_solver *h) {
   if (!h) return LMG_ERR_INVALID_ARGUMENT;
   delete h;

@@ -29,6 +29,8 @@ Periodicity parse_periodicity(const std::string &s);  // pythonify.h:38-52
 class SolverBase {
  public:
   explicit SolverBase(Periodicity x, Periodicity y, Periodicity z);
+  struct NoNBodyRules {};
+  explicit SolverBase(NoNBodyRules) {}
   virtual ~SolverBase();
 
   // NBody::setParametersNBody, mobility.h:78-97 (algorithm already parsed)
@@ -50,6 +52,8 @@ class SolverBase {
   // reference): kind "none" or "mlp" with the network's parameters
   virtual void set_preconditioner(const std::string &kind, const float *params, size_t n) = 0;
   int last_solve_iterations() const { return last_inner_iters_; }
+  // called at the end of initialize() with the seed as the caller gave it
+  virtual void on_initialized(uint64_t user_seed) { (void)user_seed; }
 
   // Mobility::LangevinVelocities, MobilityInterface.h:191-206
   void langevin(double dt, double kbt, const void *F, size_t nF, const void *T, size_t nT,
@@ -106,6 +110,8 @@ class SolverBase {
 };
 
 SolverBase *make_solver(Periodicity x, Periodicity y, Periodicity z, int precision);
+// SelfMobility (solvers/SelfMobility/mobility.h): no hydrodynamic interactions
+SolverBase *make_self_mobility(Periodicity x, Periodicity y, Periodicity z, int precision);
 
 // internal test hook: T^{1/2} e1 for a symmetric tridiagonal matrix (FP64,
 // host build of the device solver).  Returns 0 on success.

@@ -65,6 +65,7 @@ void SolverBase::initialize(double viscosity, double radius, bool include_angula
   rt0_ = 1.0 / (8.0 * M_PI * viscosity * radius * radius);
   r0_ = 1.0 / (8.0 * M_PI * viscosity * radius * radius * radius);
   // seeding chain of mobility.h:107-111 and MobilityInterface.h:106-110
+  const uint64_t user_seed = seed;
   if (seed == 0) seed = std::random_device()();
   nbody_rng_ = std::mt19937((std::mt19937::result_type)seed);
   uint64_t seed2 = nbody_rng_();
@@ -76,6 +77,7 @@ void SolverBase::initialize(double viscosity, double radius, bool include_angula
   cb_ = cb;
   cb_user_ = user;
   ang_ = include_angular;
+  on_initialized(user_seed);
 }
 
 void SolverBase::check_positions_set(const char *who) const {

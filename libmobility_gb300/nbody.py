@@ -100,6 +100,7 @@ class NBody:
     """
 
     precision = _default_precision()
+    _create = "lmg_create"
 
     def __init__(self, periodicityX, periodicityY, periodicityZ, precision=None):
         lib = _capi.load()
@@ -109,8 +110,9 @@ class NBody:
         self.precision = p
         self._h = None
         h = ctypes.c_void_p()
-        _capi.check(lib.lmg_create(str(periodicityX).encode(), str(periodicityY).encode(),
-                                   str(periodicityZ).encode(), _PRECISIONS[p], ctypes.byref(h)))
+        create = getattr(lib, self._create)
+        _capi.check(create(str(periodicityX).encode(), str(periodicityY).encode(),
+                           str(periodicityZ).encode(), _PRECISIONS[p], ctypes.byref(h)))
         self._lib = lib
         self._h = h
         self._wall = periodicityZ == "single_wall"
@@ -348,3 +350,16 @@ class NBody:
     def clean(self):
         """Frees the solver's Lanczos storage and scratch."""
         self._check(self._lib.lmg_clean(self._h))
+
+
+class SelfMobility(NBody):
+    """libMobility's SelfMobility (solvers/SelfMobility/mobility.h): no
+    hydrodynamic interactions, mobility 1/(6 pi eta a) I (and 1/(8 pi eta a^3) I
+    for rotations), computed on the host through the same C ABI."""
+
+    _create = "lmg_create_self_mobility"
+
+    def setParameters(self, parameter=None):
+        """Accepted and ignored, as in the reference (mobility.h:52-54)."""
+        return None
+
