@@ -78,6 +78,8 @@ def load():
     lib.lmg_internal_tridiag_sqrt_e1.argtypes = [_VP, _VP, _I, _VP]
     lib.lmg_internal_launch_count.restype = ctypes.c_ulonglong
     lib.lmg_internal_launch_count.argtypes = []
+    lib.lmg_internal_mdot_plan_override.restype = _I
+    lib.lmg_internal_mdot_plan_override.argtypes = [_I, _I]
     lib.lmg_internal_fma_probe.restype = _I
     lib.lmg_internal_fma_probe.argtypes = [_I, _I, _I, _VP, _VP]
     lib.lmg_internal_fma2_probe.restype = _I

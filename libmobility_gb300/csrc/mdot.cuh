@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "pack2.cuh"
 #include "rpy_pair.cuh"
 
 namespace lmg {
@@ -164,9 +165,14 @@ mdot_kernel(const MdotArgs<R> a) {
   constexpr int NC = ANG ? 6 : 3;  // accumulated components per target
   constexpr bool COMP = sizeof(R) == 4;  // compensated accumulation in FP32
 
-  __shared__ Q4<R> sp[THREADS];
-  __shared__ Q4<R> sf[HAS_F ? THREADS : 1];
-  __shared__ Q4<R> st[USE_T ? THREADS : 1];
+  // The fused FP32 wall evaluation takes two sources at a time in packed
+  // f32x2 instructions (pack2.cuh); its sources are staged as nine separate
+  // arrays so that one float4 read yields a component of four sources.
+  constexpr bool PACK = PK::FUSED_WALL;
+  __shared__ Q4<R> sp[PACK ? 1 : THREADS];
+  __shared__ Q4<R> sf[HAS_F && !PACK ? THREADS : 1];
+  __shared__ Q4<R> st[USE_T && !PACK ? THREADS : 1];
+  __shared__ __align__(16) float sv[PACK ? 9 : 1][PACK ? THREADS : 4];
   __shared__ int s_last;
 
   const int N = a.N;
@@ -237,13 +243,63 @@ mdot_kernel(const MdotArgs<R> a) {
         if (HAS_F) { fv.x = b * a.F[3 * j]; fv.y = b * a.F[3 * j + 1]; fv.z = b * a.F[3 * j + 2]; }
         if (USE_T) { tv.x = b * a.T[3 * j]; tv.y = b * a.T[3 * j + 1]; tv.z = b * a.T[3 * j + 2]; }
       }
-      sp[threadIdx.x] = p;
-      if (HAS_F) sf[threadIdx.x] = fv;
-      if (USE_T) st[threadIdx.x] = tv;
+      if constexpr (PACK) {
+        const float c9[9] = {p.x, p.y, p.z, fv.x, fv.y, fv.z, tv.x, tv.y, tv.z};
+#pragma unroll
+        for (int c = 0; c < 9; c++) sv[c][threadIdx.x] = c9[c];
+      } else {
+        sp[threadIdx.x] = p;
+        if (HAS_F) sf[threadIdx.x] = fv;
+        if (USE_T) st[threadIdx.x] = tv;
+      }
     }
     __syncthreads();
     const int n_here = min(THREADS, c_end - ts);
-    if (uniform && n_here == THREADS) {
+    if constexpr (PACK) {
+      if (uniform && n_here == THREADS) {
+        V3p u2[TPT], w2[TPT];
+#pragma unroll
+        for (int t = 0; t < TPT; t++) {
+          u2[t] = {bc(0.f), bc(0.f), bc(0.f)};
+          w2[t] = {bc(0.f), bc(0.f), bc(0.f)};
+        }
+#pragma unroll 1
+        for (int jj = 0; jj < THREADS; jj += 4) {
+          float4 q[9];
+#pragma unroll
+          for (int c = 0; c < 9; c++) q[c] = *reinterpret_cast<const float4 *>(&sv[c][jj]);
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            F2 v[9];
+#pragma unroll
+            for (int c = 0; c < 9; c++) v[c] = h ? mk2(q[c].z, q[c].w) : mk2(q[c].x, q[c].y);
+#pragma unroll
+            for (int t = 0; t < TPT; t++)
+              wall_pair_fused_x2(a.k, a.kw, bc(xi[t]), bc(yi[t]), bc(zi[t]), v[0], v[1], v[2],
+                                 v[3], v[4], v[5], v[6], v[7], v[8], u2[t], w2[t]);
+          }
+        }
+#pragma unroll
+        for (int t = 0; t < TPT; t++) {  // the two lanes hold even and odd sources
+          u[t].x += u2[t].x.v.x + u2[t].x.v.y;
+          u[t].y += u2[t].y.v.x + u2[t].y.v.y;
+          u[t].z += u2[t].z.v.x + u2[t].z.v.y;
+          w[t].x += w2[t].x.v.x + w2[t].x.v.y;
+          w[t].y += w2[t].y.v.x + w2[t].y.v.y;
+          w[t].z += w2[t].z.v.x + w2[t].z.v.y;
+        }
+      } else {
+        for (int jj = 0; jj < n_here; jj++) {
+          const int j = ts + jj;
+#pragma unroll
+          for (int t = 0; t < TPT; t++)
+            if (j >= lo[t] && j < hi[t])
+              wall_pair_fused(a.k, a.kw, xi[t], yi[t], zi[t], sv[0][jj], sv[1][jj], sv[2][jj],
+                              sv[3][jj], sv[4][jj], sv[5][jj], sv[6][jj], sv[7][jj], sv[8][jj],
+                              u[t], w[t]);
+        }
+      }
+    } else if (uniform && n_here == THREADS) {
 #pragma unroll 4
       for (int jj = 0; jj < THREADS; jj++) {
         const Q4<R> p = sp[jj];

@@ -56,7 +56,11 @@ cudaError_t mdot_plan(const MdotShape &s, int N, int max_src_span, int num_sms, 
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, 0);
   if (e != cudaSuccess) return e;
   per_sm = std::max(per_sm, 1);
-  const long want = 2L * num_sms * per_sm;  // two waves worth of CTAs
+  // two waves of CTAs, and at least 32 CTAs per SM: kernels with few
+  // resident CTAs (the wall kernel holds 5 per SM) otherwise lose a large
+  // share of the last wave; measured on wall N = 16384 / 65536, 32 splits
+  // beat 12 by 7 % and 3 by 10 %
+  const long want = std::max(2L * num_sms * per_sm, 32L * num_sms);
   int nsplit = (int)std::max(1L, (want + plan.tiles - 1) / plan.tiles);
   // at least one full source tile per split
   const int max_split = std::max(1, max_src_span / kThreads);

@@ -13,6 +13,7 @@
 
 namespace lmg {
 std::atomic<unsigned long long> g_launches{0};
+std::atomic<int> g_force_tpt{0}, g_force_split{0};
 }
 
 namespace {
@@ -60,6 +61,16 @@ __global__ void fma2_chain_kernel(int iters, float *sink) {
 extern "C" {
 
 unsigned long long lmg_internal_launch_count(void) { return lmg::g_launches.load(); }
+
+// Forces targets-per-thread (1 or 2) and the source split count of every
+// all-pairs launch planned after the call; 0 restores the planner's choice.
+// Plans cached by existing solvers are re-made on their next call.
+int lmg_internal_mdot_plan_override(int tpt, int nsplit) {
+  if (tpt < 0 || tpt > 2 || nsplit < 0 || nsplit > 65535) return 1;
+  lmg::g_force_tpt.store(tpt);
+  lmg::g_force_split.store(nsplit);
+  return 0;
+}
 
 // Launches blocks x threads of the FMA chain on `stream`; flops performed =
 // blocks * threads * iters * 64 * 2.

@@ -282,14 +282,16 @@ void Solver<R>::mdot_device(const R *pos, const R *F, const R *T, R *U, R *W) {
     if (W) LMG_CUDA(cudaMemsetAsync(W, 0, 3 * (size_t)N * sizeof(R), stream()));
     return;
   }
-  const long key = ((long)N << 8) | (s.geom << 3) | (s.has_f << 2) | (s.has_t << 1) | s.ang;
+  const int ftpt = g_force_tpt.load(), fsplit = g_force_split.load();
+  const long key = ((long)N << 30) | ((long)fsplit << 10) | (ftpt << 8) | (s.geom << 3) |
+                   (s.has_f << 2) | (s.has_t << 1) | s.ang;
   auto it = plans_.find(key);
   if (it == plans_.end() || it->second.tiles == 0) {
     MdotPlan plan;
     // span depends on the tile width, which the plan picks: plan twice
-    LMG_CUDA(mdot_plan<R>(s, N, N, sms(), 0, 0, plan));
+    LMG_CUDA(mdot_plan<R>(s, N, N, sms(), ftpt, fsplit, plan));
     const int span = mdot_max_span(N, nper, nullptr, 0, plan.threads * plan.tpt);
-    LMG_CUDA(mdot_plan<R>(s, N, span, sms(), plan.tpt, 0, plan));
+    LMG_CUDA(mdot_plan<R>(s, N, span, sms(), plan.tpt, fsplit, plan));
     it = plans_.insert_or_assign(key, plan).first;
   }
   const MdotPlan &plan = it->second;

@@ -89,6 +89,36 @@ def test_random_systems_vs_oracle(cuda, oracle, precision, wall, blocks):
 
 
 @pytest.mark.parametrize("precision", ["float", "double"])
+@pytest.mark.parametrize("wall", [0, 1])
+def test_every_launch_plan_agrees(cuda, oracle, precision, wall):
+    """Targets per thread (1, 2) and source splits (1, 3, 8, planner's) only
+    change the order of summation: every plan matches the oracle.  The wall
+    case with all blocks runs the packed two-sources-at-a-time evaluation,
+    with overlapping pairs (r < 2a) and particles below the radius mixed in."""
+    from libmobility_gb300 import _capi
+    lib = _capi.load()
+    rng = np.random.default_rng(21 + wall)
+    cases = ((1537, 1537), (3000, 1000))
+    try:
+        for N, nper in cases:
+            p = _system(rng, N, wall, phi=0.15)
+            F = rng.normal(size=(N, 3))
+            T = rng.normal(size=(N, 3))
+            Uo, Wo = oracle.mdot(p, F, T, a=1.1, viscosity=0.9, wall=wall, include_angular=1,
+                                 nper_batch=nper)
+            for tpt in (1, 2):
+                for split in (0, 1, 3, 8):
+                    assert lib.lmg_internal_mdot_plan_override(tpt, split) == 0
+                    s = make_solver(wall, 1, 1.1, 0.9, precision, N, nper)
+                    s.setPositions(p)
+                    U, W = s.Mdot(F, T)
+                    assert rel_err(U, Uo) <= TOL[precision], (N, tpt, split)
+                    assert rel_err(W, Wo) <= TOL[precision], (N, tpt, split)
+    finally:
+        lib.lmg_internal_mdot_plan_override(0, 0)
+
+
+@pytest.mark.parametrize("precision", ["float", "double"])
 def test_large_open_and_wall_subsample(cuda, oracle, precision):
     """N = 4096 open (UF) and N = 16384 wall (all blocks): rows 0..511 against
     the FP64 oracle summed over every source."""
