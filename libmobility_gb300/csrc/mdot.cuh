@@ -88,43 +88,56 @@ template <class R, int GEOM, bool HAS_F, bool HAS_T, bool ANG> struct PairKernel
   static constexpr bool FUSED_WALL =
       GEOM == kWall && UF && UT && WT && WF && sizeof(R) == 4;
 
-  // Adds the contribution of source (p, f, t) to target (x, y, z).
-  static __device__ __forceinline__ void eval(const PairConst<R> &k, const WallConst &kw, R xi,
-                                              R yi, R zi, const Q4<R> &p, const Q4<R> &fv,
-                                              const Q4<R> &tv, Vec3<R> &u, Vec3<R> &w) {
+  // Adds the contribution of source (p, f, t) to target (x, y, z) and
+  // returns the squared scaled distance r^2.  EXACT = false is the fast form
+  // used for every pair of a full tile: the RPY coefficients are those of
+  // separated pairs taken at max(r^2, 4) (so the value is finite and O(1)
+  // for an overlapping or self pair, and exact for r >= 2a), and the wall
+  // images take the pair formula even for the self pair.  The caller
+  // replaces the fast value by the exact one for the pairs with r^2 < 4
+  // (correct() below).
+  template <bool EXACT = true>
+  static __device__ __forceinline__ R eval(const PairConst<R> &k, const WallConst &kw, R xi,
+                                           R yi, R zi, const Q4<R> &p, const Q4<R> &fv,
+                                           const Q4<R> &tv, Vec3<R> &u, Vec3<R> &w) {
     if constexpr (FUSED_WALL) {
       wall_pair_fused(k, kw, xi, yi, zi, p.x, p.y, p.z, fv.x, fv.y, fv.z, tv.x, tv.y, tv.z, u,
                       w);
-      return;
+      return R(4);
     }
     const R dx = xi - p.x;
     const R dy = yi - p.y;
     const R dz = zi - p.z;
-    const R r2 = dx * dx + dy * dy + dz * dz;
-    const R ir = dev_rsqrt<R>(r2);
+    const R r2 = fmaR(dx, dx, fmaR(dy, dy, dz * dz));
     R f = 0, G = 0, fw = 0, Gw = 0, c = 0;
-    rpy_coefficients<R, UF, WT, UT || WF>(k, r2, ir, f, G, fw, Gw, c);
+    if constexpr (EXACT) {
+      rpy_coefficients<R, UF, WT, UT || WF, true>(k, r2, dev_rsqrt<R>(r2), f, G, fw, Gw, c);
+    } else {
+      const R r2c = r2 > R(4) ? r2 : R(4);
+      rpy_coefficients<R, UF, WT, UT || WF, false>(k, r2c, rsqrt_normal<R>(r2c), f, G, fw, Gw,
+                                                   c);
+    }
     if (UF) {
-      const R g = G * (dx * fv.x + dy * fv.y + dz * fv.z);
-      u.x += f * fv.x + g * dx;
-      u.y += f * fv.y + g * dy;
-      u.z += f * fv.z + g * dz;
+      const R g = G * fmaR(dx, fv.x, fmaR(dy, fv.y, dz * fv.z));
+      u.x = fmaR(f, fv.x, fmaR(g, dx, u.x));
+      u.y = fmaR(f, fv.y, fmaR(g, dy, u.y));
+      u.z = fmaR(f, fv.z, fmaR(g, dz, u.z));
     }
     if (UT) {  // c (T x d)
-      u.x += c * (tv.y * dz - tv.z * dy);
-      u.y += c * (tv.z * dx - tv.x * dz);
-      u.z += c * (tv.x * dy - tv.y * dx);
+      u.x = fmaR(c, fmaR(tv.y, dz, -tv.z * dy), u.x);
+      u.y = fmaR(c, fmaR(tv.z, dx, -tv.x * dz), u.y);
+      u.z = fmaR(c, fmaR(tv.x, dy, -tv.y * dx), u.z);
     }
     if (WT) {
-      const R g = Gw * (dx * tv.x + dy * tv.y + dz * tv.z);
-      w.x += fw * tv.x + g * dx;
-      w.y += fw * tv.y + g * dy;
-      w.z += fw * tv.z + g * dz;
+      const R g = Gw * fmaR(dx, tv.x, fmaR(dy, tv.y, dz * tv.z));
+      w.x = fmaR(fw, tv.x, fmaR(g, dx, w.x));
+      w.y = fmaR(fw, tv.y, fmaR(g, dy, w.y));
+      w.z = fmaR(fw, tv.z, fmaR(g, dz, w.z));
     }
     if (WF) {  // c (F x d)
-      w.x += c * (fv.y * dz - fv.z * dy);
-      w.y += c * (fv.z * dx - fv.x * dz);
-      w.z += c * (fv.x * dy - fv.y * dx);
+      w.x = fmaR(c, fmaR(fv.y, dz, -fv.z * dy), w.x);
+      w.y = fmaR(c, fmaR(fv.z, dx, -fv.x * dz), w.y);
+      w.z = fmaR(c, fmaR(fv.x, dy, -fv.y * dx), w.z);
     }
     if (GEOM == kWall) {
       // image vector R = (dx, dy, h_i + h_j), shared by all blocks
@@ -134,7 +147,7 @@ template <class R, int GEOM, bool HAS_F, bool HAS_T, bool ANG> struct PairKernel
       Vec3<R> cu = {0, 0, 0}, cw = {0, 0, 0}, ct = {0, 0, 0}, cf = {0, 0, 0};
       const Vec3<R> F3 = {fv.x, fv.y, fv.z};
       const Vec3<R> T3 = {tv.x, tv.y, tv.z};
-      if (r2 > R(0)) {
+      if (!EXACT || r2 > R(0)) {
         const R iRz = dev_div<R>(R(1), Rz);
         const R hj = p.z * iRz;  // h_j / R_z
         if (UF) wall_uf_pair<R>(ex, ey, ez, iR, hj, F3, cu);
@@ -153,6 +166,23 @@ template <class R, int GEOM, bool HAS_F, bool HAS_T, bool ANG> struct PairKernel
       if (WT) { w.x += k.r0 * cw.x; w.y += k.r0 * cw.y; w.z += k.r0 * cw.z; }
       if (WF) { w.x += k.rt0 * cf.x; w.y += k.rt0 * cf.y; w.z += k.rt0 * cf.z; }
     }
+    return r2;
+  }
+
+  // For a pair with r^2 < 4 already added in the fast form: adds
+  // (exact - fast).  Both are O(1) there, so the difference is accurate.
+  static __device__ __forceinline__ void correct(const PairConst<R> &k, const WallConst &kw,
+                                                 R xi, R yi, R zi, const Q4<R> &p,
+                                                 const Q4<R> &fv, const Q4<R> &tv, Vec3<R> &u,
+                                                 Vec3<R> &w) {
+    const R dx = xi - p.x, dy = yi - p.y, dz = zi - p.z;
+    if (fmaR(dx, dx, fmaR(dy, dy, dz * dz)) < R(4)) {
+      Vec3<R> ue = {0, 0, 0}, we = {0, 0, 0}, uf = {0, 0, 0}, wf = {0, 0, 0};
+      eval<true>(k, kw, xi, yi, zi, p, fv, tv, ue, we);
+      eval<false>(k, kw, xi, yi, zi, p, fv, tv, uf, wf);
+      u.x += ue.x - uf.x; u.y += ue.y - uf.y; u.z += ue.z - uf.z;
+      w.x += we.x - wf.x; w.y += we.y - wf.y; w.z += we.z - wf.z;
+    }
   }
 };
 
@@ -165,14 +195,20 @@ mdot_kernel(const MdotArgs<R> a) {
   constexpr int NC = ANG ? 6 : 3;  // accumulated components per target
   constexpr bool COMP = sizeof(R) == 4;  // compensated accumulation in FP32
 
-  // The fused FP32 wall evaluation takes two sources at a time in packed
-  // f32x2 instructions (pack2.cuh); its sources are staged as nine separate
-  // arrays so that one float4 read yields a component of four sources.
+  // The fused FP32 wall evaluation (all blocks) and the FP32 open UF
+  // evaluation take two sources at a time in packed f32x2 instructions
+  // (pack2.cuh); their sources are staged as separate arrays (x, y, z, F,
+  // and T for the wall) so that one float4 read yields a component of four
+  // sources.
   constexpr bool PACK = PK::FUSED_WALL;
-  __shared__ Q4<R> sp[PACK ? 1 : THREADS];
-  __shared__ Q4<R> sf[HAS_F && !PACK ? THREADS : 1];
-  __shared__ Q4<R> st[USE_T && !PACK ? THREADS : 1];
-  __shared__ __align__(16) float sv[PACK ? 9 : 1][PACK ? THREADS : 4];
+  constexpr bool PACK_OPEN =
+      GEOM == kOpen && sizeof(R) == 4 && HAS_F && !ANG && THREADS % 32 == 0;
+  constexpr int NSV = PACK ? 9 : (PACK_OPEN ? 6 : 1);
+  constexpr bool SOA = PACK || PACK_OPEN;
+  __shared__ Q4<R> sp[SOA ? 1 : THREADS];
+  __shared__ Q4<R> sf[HAS_F && !SOA ? THREADS : 1];
+  __shared__ Q4<R> st[USE_T && !SOA ? THREADS : 1];
+  __shared__ __align__(16) float sv[NSV][SOA ? THREADS : 4];
   __shared__ int s_last;
 
   const int N = a.N;
@@ -243,10 +279,10 @@ mdot_kernel(const MdotArgs<R> a) {
         if (HAS_F) { fv.x = b * a.F[3 * j]; fv.y = b * a.F[3 * j + 1]; fv.z = b * a.F[3 * j + 2]; }
         if (USE_T) { tv.x = b * a.T[3 * j]; tv.y = b * a.T[3 * j + 1]; tv.z = b * a.T[3 * j + 2]; }
       }
-      if constexpr (PACK) {
+      if constexpr (SOA) {
         const float c9[9] = {p.x, p.y, p.z, fv.x, fv.y, fv.z, tv.x, tv.y, tv.z};
 #pragma unroll
-        for (int c = 0; c < 9; c++) sv[c][threadIdx.x] = c9[c];
+        for (int c = 0; c < NSV; c++) sv[c][threadIdx.x] = c9[c];
       } else {
         sp[threadIdx.x] = p;
         if (HAS_F) sf[threadIdx.x] = fv;
@@ -299,14 +335,104 @@ mdot_kernel(const MdotArgs<R> a) {
                               u[t], w[t]);
         }
       }
-    } else if (uniform && n_here == THREADS) {
-#pragma unroll 4
-      for (int jj = 0; jj < THREADS; jj++) {
-        const Q4<R> p = sp[jj];
-        const Q4<R> fv = HAS_F ? sf[jj] : Q4<R>{0, 0, 0, 0};
-        const Q4<R> tv = USE_T ? st[jj] : Q4<R>{0, 0, 0, 0};
+    } else if constexpr (PACK_OPEN) {
+      if (uniform && n_here == THREADS) {
+        // as the scalar full-tile path below, two sources per instruction
+#pragma unroll 1
+        for (int j0 = 0; j0 < THREADS; j0 += 32) {
+          V3p u2[TPT];
+          float2 mr2[TPT];
 #pragma unroll
-        for (int t = 0; t < TPT; t++) PK::eval(a.k, a.kw, xi[t], yi[t], zi[t], p, fv, tv, u[t], w[t]);
+          for (int t = 0; t < TPT; t++) {
+            u2[t] = {bc(0.f), bc(0.f), bc(0.f)};
+            mr2[t] = make_float2(4.f, 4.f);
+          }
+#pragma unroll 2
+          for (int jj = j0; jj < j0 + 32; jj += 4) {
+            float4 q[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) q[c] = *reinterpret_cast<const float4 *>(&sv[c][jj]);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+              F2 v[6];
+#pragma unroll
+              for (int c = 0; c < 6; c++) v[c] = h ? mk2(q[c].z, q[c].w) : mk2(q[c].x, q[c].y);
+#pragma unroll
+              for (int t = 0; t < TPT; t++)
+                open_uf_pair_x2(a.k, bc(xi[t]), bc(yi[t]), bc(zi[t]), v[0], v[1], v[2], v[3],
+                                v[4], v[5], u2[t], mr2[t]);
+            }
+          }
+          bool near = false;
+#pragma unroll
+          for (int t = 0; t < TPT; t++) {
+            u[t].x += u2[t].x.v.x + u2[t].x.v.y;
+            u[t].y += u2[t].y.v.x + u2[t].y.v.y;
+            u[t].z += u2[t].z.v.x + u2[t].z.v.y;
+            near = near || fminf(mr2[t].x, mr2[t].y) < 4.f;
+          }
+          if (__any_sync(0xffffffffu, near)) {
+#pragma unroll
+            for (int t = 0; t < TPT; t++) {
+              if (fminf(mr2[t].x, mr2[t].y) < 4.f) {
+                for (int jj = j0; jj < j0 + 32; jj++) {
+                  const Q4<R> p = {sv[0][jj], sv[1][jj], sv[2][jj], 0};
+                  const Q4<R> fv = {sv[3][jj], sv[4][jj], sv[5][jj], 0};
+                  PK::correct(a.k, a.kw, xi[t], yi[t], zi[t], p, fv, fv, u[t], w[t]);
+                }
+              }
+            }
+          }
+        }
+      } else {
+        for (int jj = 0; jj < n_here; jj++) {
+          const int j = ts + jj;
+          const Q4<R> p = {sv[0][jj], sv[1][jj], sv[2][jj], 0};
+          const Q4<R> fv = {sv[3][jj], sv[4][jj], sv[5][jj], 0};
+#pragma unroll
+          for (int t = 0; t < TPT; t++)
+            if (j >= lo[t] && j < hi[t]) PK::eval(a.k, a.kw, xi[t], yi[t], zi[t], p, fv, fv, u[t], w[t]);
+        }
+      }
+    } else if (uniform && n_here == THREADS) {
+      // Fast form for every pair, 32 sources at a time; then, in a warp where
+      // some target met a pair closer than 2a among those 32 (its self pair,
+      // or an overlap), those targets swap the fast value of such pairs for
+      // the exact one.  Targets are tile-aligned, so a warp's self pairs all
+      // fall in the same 32 sources.
+#pragma unroll 1
+      for (int j0 = 0; j0 < THREADS; j0 += 32) {
+        R mr2[TPT];
+#pragma unroll
+        for (int t = 0; t < TPT; t++) mr2[t] = R(4);
+#pragma unroll 4
+        for (int jj = j0; jj < j0 + 32; jj++) {
+          const Q4<R> p = sp[jj];
+          const Q4<R> fv = HAS_F ? sf[jj] : Q4<R>{0, 0, 0, 0};
+          const Q4<R> tv = USE_T ? st[jj] : Q4<R>{0, 0, 0, 0};
+#pragma unroll
+          for (int t = 0; t < TPT; t++) {
+            const R r2 = PK::template eval<false>(a.k, a.kw, xi[t], yi[t], zi[t], p, fv, tv,
+                                                  u[t], w[t]);
+            mr2[t] = r2 < mr2[t] ? r2 : mr2[t];  // a min in R (no promotion)
+          }
+        }
+        bool near = false;
+#pragma unroll
+        for (int t = 0; t < TPT; t++) near = near || mr2[t] < R(4);
+        if (__any_sync(0xffffffffu, near)) {
+#pragma unroll
+          for (int t = 0; t < TPT; t++) {
+            if (mr2[t] < R(4)) {
+              for (int jj = j0; jj < j0 + 32; jj++) {
+                const Q4<R> p = sp[jj];
+                const Q4<R> fv = HAS_F ? sf[jj] : Q4<R>{0, 0, 0, 0};
+                const Q4<R> tv = USE_T ? st[jj] : Q4<R>{0, 0, 0, 0};
+                PK::correct(a.k, a.kw, xi[t], yi[t], zi[t], p, fv, tv, u[t], w[t]);
+              }
+            }
+          }
+        }
       }
     } else {
       for (int jj = 0; jj < n_here; jj++) {
@@ -380,14 +506,31 @@ mdot_kernel(const MdotArgs<R> a) {
     R Ss[NC], Cs[NC];
 #pragma unroll
     for (int c = 0; c < NC; c++) { Ss[c] = 0; Cs[c] = 0; }
-    for (int s = 0; s < nsplit; s++) {
-      const R *ps = base + (size_t)s * (2 * NC) * BT;
+    // UNR splits' partials are loaded before any is folded, so that many L2
+    // reads are in flight at once (the fold order stays the split order)
+    constexpr int UNR = 24 / NC;
+    for (int s0 = 0; s0 < nsplit; s0 += UNR) {
+      R sv[UNR][NC], cv[UNR][NC];
 #pragma unroll
-      for (int c = 0; c < NC; c++) {
-        const R sv = __ldcg(ps + (size_t)c * BT + l);
-        const R cv = __ldcg(ps + (size_t)(NC + c) * BT + l);
-        if (COMP) fold(Ss[c], Cs[c], sv); else Ss[c] += sv;
-        Cs[c] += cv;
+      for (int u = 0; u < UNR; u++) {
+        // past the last split: re-read the last one (a valid address), add 0
+        const bool in = s0 + u < nsplit;
+        const R *ps = base + (size_t)(in ? s0 + u : nsplit - 1) * (2 * NC) * BT;
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+          const R sl = __ldcg(ps + (size_t)c * BT + l);
+          const R cl = __ldcg(ps + (size_t)(NC + c) * BT + l);
+          sv[u][c] = in ? sl : R(0);
+          cv[u][c] = in ? cl : R(0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UNR; u++) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+          if (COMP) fold(Ss[c], Cs[c], sv[u][c]); else Ss[c] += sv[u][c];
+          Cs[c] += cv[u][c];
+        }
       }
     }
     if (i < N) {

@@ -137,4 +137,28 @@ __device__ __forceinline__ void wall_pair_fused_x2(
   u.z = fms2(k1, fma2(dy, Tx, neg2(dx * Ty)), fma2(mp, ez, fma2(pv, f2i, u.z)));
 }
 
+// Packed open-space UF pair (translational RPY, forces only) in the fast
+// form of PairKernel::eval<false> (mdot.cuh): r^2 clamped at 4 for the
+// coefficients, so overlapping and self pairs give finite values that the
+// caller corrects; the smallest unclamped r^2 of each lane is kept in mr2.
+// Same formulas and order of operations per lane as the scalar fast form.
+__device__ __forceinline__ void open_uf_pair_x2(const PairConst<float> &k, F2 xi, F2 yi, F2 zi,
+                                                F2 Xj, F2 Yj, F2 Zj, F2 Fx, F2 Fy, F2 Fz,
+                                                V3p &u, float2 &mr2) {
+  const F2 dx = xi - Xj, dy = yi - Yj, dz = zi - Zj;
+  const F2 r2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
+  mr2.x = fminf(mr2.x, r2.v.x);
+  mr2.y = fminf(mr2.y, r2.v.y);
+  const F2 ir = mk2(rsqrt_normal<float>(fmaxf(r2.v.x, 4.0f)),
+                    rsqrt_normal<float>(fmaxf(r2.v.y, 4.0f)));
+  const F2 ir2 = ir * ir;
+  const F2 ir3 = ir * ir2;
+  const F2 f = ir * fma2(bc(k.tf1), ir2, bc(k.tf0));
+  const F2 G = ir3 * fma2(bc(k.tg1), ir2, bc(k.tg0));
+  const F2 g = G * fma2(dx, Fx, fma2(dy, Fy, dz * Fz));
+  u.x = fma2(f, Fx, fma2(g, dx, u.x));
+  u.y = fma2(f, Fy, fma2(g, dy, u.y));
+  u.z = fma2(f, Fz, fma2(g, dz, u.z));
+}
+
 }  // namespace lmg

@@ -32,6 +32,20 @@ template <class R> __device__ __forceinline__ R dev_rsqrt(R x);
 template <> __device__ __forceinline__ float dev_rsqrt<float>(float x) { return rsqrtf(x); }
 template <> __device__ __forceinline__ double dev_rsqrt<double>(double x) { return rsqrt(x); }
 
+// Reciprocal square root for arguments known to be normal numbers (r^2
+// clamped at 4): the hardware approximation without the subnormal handling.
+template <class R> __device__ __forceinline__ R rsqrt_normal(R x);
+template <> __device__ __forceinline__ float rsqrt_normal<float>(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+template <> __device__ __forceinline__ double rsqrt_normal<double>(double x) { return rsqrt(x); }
+
+template <class R> __device__ __forceinline__ R fmaR(R a, R b, R c);
+template <> __device__ __forceinline__ float fmaR<float>(float a, float b, float c) { return fmaf(a, b, c); }
+template <> __device__ __forceinline__ double fmaR<double>(double a, double b, double c) { return fma(a, b, c); }
+
 // Multiplication that the compiler may not contract into an FMA with a
 // following subtraction: targets and sources are scaled by 1/a with it, so a
 // particle paired with itself (or with a coincident one) yields exactly d = 0.
@@ -84,7 +98,9 @@ inline PairConst<R> make_pair_const(double t0, double r0, double rt0) {
 // r^2, ir = 1/r).  U_UF = f F + G (d.F) d ; W_WT = fw T + Gw (d.T) d ;
 // coupling c:  U_UT = c (T x d), W_WF = c (F x d).  Self pair (r2 == 0):
 // f = t0, fw = r0, G = Gw = c = 0 (d = 0 makes the coupling vanish anyway).
-template <class R, bool TT, bool ROT, bool CPL>
+// NEAR = false evaluates the far-field formulas for every pair (callers that
+// detect r < 2a themselves and redo those pairs).
+template <class R, bool TT, bool ROT, bool CPL, bool NEAR = true>
 __device__ __forceinline__ void rpy_coefficients(const PairConst<R> &k, R r2, R ir,
                                                  R &f, R &G, R &fw, R &Gw, R &c) {
   const R ir2 = ir * ir;
@@ -98,7 +114,7 @@ __device__ __forceinline__ void rpy_coefficients(const PairConst<R> &k, R r2, R 
     Gw = k.rg1 * ir3 * ir2;
   }
   if (CPL) c = k.rt0 * ir3;
-  if (r2 < R(4)) {  // overlapping pair (r < 2a), rare except the self pair
+  if (NEAR && r2 < R(4)) {  // overlapping pair (r < 2a), rare except the self pair
     const bool self = !(r2 > R(0));
     const R r = self ? R(0) : r2 * ir;
     const R irs = self ? R(0) : ir;
