@@ -216,6 +216,54 @@ lmg_status lmg_mdot_noalloc_f32(const float *pos, const float *F, const float *T
                                 double hydrodynamicRadius, int includeAngular,
                                 void *cuda_stream, char *err, size_t err_len);
 
+/* ------------------------------------------------------------------------
+ * Ensembles: no counterpart in the reference, whose NBody batches
+ * (Nbatch x NperBatch, mobility.h:52-60) are equal in size and share one
+ * geometry.  An ensemble holds many independent systems of uneven size, each
+ * open or above its own bottom wall, with one viscosity and radius, forces
+ * only (no torques).  Every system behaves as its own NBody solver; Mdot and
+ * sqrtMdotW run all systems together: one all-pairs launch per group of
+ * systems of the same geometry and size bucket per matrix-vector product,
+ * one launch for all systems' Lanczos vector updates, each system stopping
+ * at its own convergence (LanczosAlgorithm.cu:202-222 per system).
+ * Buffers follow the conventions above, all systems concatenated in the
+ * order given to lmg_ensemble_set_systems (3 values per particle).
+ * ------------------------------------------------------------------------ */
+typedef struct lmg_ensemble lmg_ensemble;
+
+lmg_status lmg_ensemble_create(int precision, lmg_ensemble **out);
+lmg_status lmg_ensemble_destroy(lmg_ensemble *h);
+const char *lmg_ensemble_last_error(const lmg_ensemble *h);
+/* As lmg_set_stream. */
+lmg_status lmg_ensemble_set_stream(lmg_ensemble *h, void *cuda_stream);
+/* sizes[s] >= 1 particles; geometry[s] 0 = open, 1 = bottom wall;
+ * wall_heights (may be NULL: 0) gives the wall position of wall systems
+ * (ignored for open ones), as NBody's wallHeight. */
+lmg_status lmg_ensemble_set_systems(lmg_ensemble *h, int nsys, const int *sizes,
+                                    const int *geometry, const double *wall_heights);
+/* As lmg_initialize without includeAngular.  autotune != 0 times the
+ * candidate launch plans of each group of systems on first use and keeps the
+ * fastest (plans differ only in summation order); 0 keeps the planner's. */
+lmg_status lmg_ensemble_initialize(lmg_ensemble *h, double viscosity,
+                                   double hydrodynamicRadius, double tolerance, uint64_t seed,
+                                   int autotune);
+/* As lmg_set_positions: every wall system is shifted by its wall height and
+ * checked against its wall ("fallen below the wall"). */
+lmg_status lmg_ensemble_set_positions(lmg_ensemble *h, const void *pos, size_t n);
+/* U = M F per system; U is overwritten. */
+lmg_status lmg_ensemble_mdot(lmg_ensemble *h, const void *F, size_t nF, void *U, size_t nU);
+/* U += prefactor * M^{1/2} dW per system (dW NULL: noise drawn as
+ * lmg_sqrt_mdot_w does, one stream for the whole ensemble).  Per system (in
+ * the caller's order, each array may be NULL): Lanczos iterations, last
+ * successive-iterate error, and the host time in ms from the start of the
+ * call until that system's result was known. */
+lmg_status lmg_ensemble_sqrt_mdot_w(lmg_ensemble *h, const void *dW, size_t ndW, void *U,
+                                    size_t nU, double prefactor, int *iterations,
+                                    double *errors, double *completion_ms);
+/* Groups, their chosen plans and the timings behind them, as JSON text
+ * (written to buf, at most len bytes with the terminating 0). */
+lmg_status lmg_ensemble_describe(const lmg_ensemble *h, char *buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,6 +28,7 @@ UNITS = [
     ("probes.cu", [], "probes.o"),
     ("noalloc.cu", [], "noalloc.o"),
     ("precond.cu", [], "precond.o"),
+    ("ensemble.cu", [], "ensemble.o"),
     ("solver_base.cpp", [], "solver_base.o"),
     ("capi.cpp", [], "capi.o"),
     ("self_mobility.cpp", [], "self_mobility.o"),

@@ -54,6 +54,16 @@ SIGNATURES = {
     "lmg_get_preconditioner_solve_iterations": (_I, [_VP, ctypes.POINTER(_I)]),
     "lmg_mdot_noalloc_f32": (_I, [_VP, _VP, _VP, _VP, _VP, ctypes.c_int64, ctypes.c_int64, _I,
                                  _D, _D, _I, _VP, ctypes.c_char_p, _SZ]),
+    "lmg_ensemble_create": (_I, [_I, ctypes.POINTER(_VP)]),
+    "lmg_ensemble_destroy": (_I, [_VP]),
+    "lmg_ensemble_last_error": (ctypes.c_char_p, [_VP]),
+    "lmg_ensemble_set_stream": (_I, [_VP, _VP]),
+    "lmg_ensemble_set_systems": (_I, [_VP, _I, _VP, _VP, _VP]),
+    "lmg_ensemble_initialize": (_I, [_VP, _D, _D, _D, ctypes.c_uint64, _I]),
+    "lmg_ensemble_set_positions": (_I, [_VP, _VP, _SZ]),
+    "lmg_ensemble_mdot": (_I, [_VP, _VP, _SZ, _VP, _SZ]),
+    "lmg_ensemble_sqrt_mdot_w": (_I, [_VP, _VP, _SZ, _VP, _SZ, _D, _VP, _VP, _VP]),
+    "lmg_ensemble_describe": (_I, [_VP, ctypes.c_char_p, _SZ]),
 }
 
 _lib = None
@@ -103,14 +113,15 @@ def load():
     return lib
 
 
-def check(status, handle=None):
+def check(status, handle=None, ensemble=False):
     """Raise RuntimeError with the library's message for a failed call (the
     reference's exceptions surface as RuntimeError through nanobind)."""
     if status == LMG_OK:
         return
     lib = load()
     if handle is not None:
-        msg = lib.lmg_last_error(handle).decode()
+        get = lib.lmg_ensemble_last_error if ensemble else lib.lmg_last_error
+        msg = get(handle).decode()
     else:
         msg = lib.lmg_create_error().decode()
     err = RuntimeError(msg or STATUS_NAMES.get(status, str(status)))

@@ -1,19 +1,25 @@
 // extern "C" boundary: every entry point of include/libmobility_gb300.h.
 // Exceptions never cross it; they become an lmg_status plus a message.
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <string>
 
+#include "ensemble.hpp"
 #include "solver.hpp"
 
 struct lmg_solver {
   std::unique_ptr<lmg::SolverBase> impl;
 };
 
+struct lmg_ensemble {
+  std::unique_ptr<lmg::EnsembleBase> impl;
+};
+
 namespace {
 thread_local std::string g_create_error;
 
-template <class F> lmg_status guarded(lmg_solver *h, F &&f) {
+template <class H, class F> lmg_status guarded(H *h, F &&f) {
   if (!h || !h->impl) return LMG_ERR_INVALID_ARGUMENT;
   try {
     f(*h->impl);
@@ -208,6 +214,84 @@ const char *lmg_precision_name(const lmg_solver *h) {
 // symmetric tridiagonal matrix with the solver's own QL routine, on the host.
 int lmg_internal_tridiag_sqrt_e1(const double *alpha, const double *beta, int m, double *out) {
   return lmg::tridiag_sqrt_e1_host(alpha, beta, m, out);
+}
+
+
+lmg_status lmg_ensemble_create(int precision, lmg_ensemble **out) {
+  if (!out) return LMG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  try {
+    auto *h = new lmg_ensemble;
+    h->impl.reset(lmg::make_ensemble(precision));
+    *out = h;
+    g_create_error.clear();
+    return LMG_OK;
+  } catch (const lmg::Error &e) {
+    g_create_error = e.what();
+    return e.code;
+  } catch (const std::exception &e) {
+    g_create_error = e.what();
+    return LMG_ERR_INTERNAL;
+  }
+}
+
+lmg_status lmg_ensemble_destroy(lmg_ensemble *h) {
+  delete h;
+  return LMG_OK;
+}
+
+const char *lmg_ensemble_last_error(const lmg_ensemble *h) {
+  if (!h || !h->impl) return "invalid handle";
+  return h->impl->last_error.c_str();
+}
+
+lmg_status lmg_ensemble_set_stream(lmg_ensemble *h, void *s) {
+  return guarded(h, [&](lmg::EnsembleBase &m) {
+    if (s == LMG_OWN_STREAM)
+      m.use_own_stream();
+    else
+      m.set_stream((cudaStream_t)s);
+  });
+}
+
+lmg_status lmg_ensemble_set_systems(lmg_ensemble *h, int nsys, const int *sizes,
+                                    const int *geometry, const double *wall_heights) {
+  return guarded(h, [&](lmg::EnsembleBase &m) {
+    m.set_systems(nsys, sizes, geometry, wall_heights);
+  });
+}
+
+lmg_status lmg_ensemble_initialize(lmg_ensemble *h, double viscosity,
+                                   double hydrodynamicRadius, double tolerance, uint64_t seed,
+                                   int autotune) {
+  return guarded(h, [&](lmg::EnsembleBase &m) {
+    m.initialize(viscosity, hydrodynamicRadius, tolerance, seed, autotune != 0);
+  });
+}
+
+lmg_status lmg_ensemble_set_positions(lmg_ensemble *h, const void *pos, size_t n) {
+  return guarded(h, [&](lmg::EnsembleBase &m) { m.set_positions(pos, n); });
+}
+
+lmg_status lmg_ensemble_mdot(lmg_ensemble *h, const void *F, size_t nF, void *U, size_t nU) {
+  return guarded(h, [&](lmg::EnsembleBase &m) { m.mdot(F, nF, U, nU); });
+}
+
+lmg_status lmg_ensemble_sqrt_mdot_w(lmg_ensemble *h, const void *dW, size_t ndW, void *U,
+                                    size_t nU, double prefactor, int *iterations,
+                                    double *errors, double *completion_ms) {
+  return guarded(h, [&](lmg::EnsembleBase &m) {
+    m.sqrt_mdot_w(dW, ndW, U, nU, prefactor, iterations, errors, completion_ms);
+  });
+}
+
+lmg_status lmg_ensemble_describe(const lmg_ensemble *h, char *buf, size_t len) {
+  if (!h || !h->impl || !buf || len == 0) return LMG_ERR_INVALID_ARGUMENT;
+  const std::string d = h->impl->describe();
+  const size_t k = std::min(len - 1, d.size());
+  std::memcpy(buf, d.data(), k);
+  buf[k] = 0;
+  return d.size() < len ? LMG_OK : LMG_ERR_INVALID_ARGUMENT;
 }
 
 }  // extern "C"

@@ -51,6 +51,10 @@ template <class R> struct MdotArgs {
   WallConst kw;          // fused all-blocks wall constants (FP32 path)
   R *part;               // scratch: [tiles][nsplit][2*NC][BT]
   unsigned *ticket;      // scratch: [tiles]
+  // optional per-batch flags (nsys entries, with sys_begin): a tile whose
+  // batches are all flagged 0 is skipped by every one of its CTAs (outputs
+  // left as they were, scratch and ticket untouched)
+  const int *sys_active;
 };
 
 // Two-sum fold of t into (S, C): S + C carries the running sum to about
@@ -247,6 +251,11 @@ mdot_kernel(const MdotArgs<R> a) {
   const int src_lo = system_start(a, s_first);
   const int src_hi = system_end(a, s_lastb);
   const bool uniform = (s_first == s_lastb);
+  if (a.sys_active != nullptr) {
+    int any = 0;
+    for (int q = s_first; q <= s_lastb; q++) any |= __ldg(a.sys_active + q);
+    if (!any) return;
+  }
   const int c_begin = src_lo + split * a.chunk;
   const int c_end = min(src_hi, c_begin + a.chunk);
 
