@@ -264,6 +264,112 @@ def sqrtmdotw_comparison(torch, steps, warmup, rank, N=65536):
     return out
 
 
+def ensemble_systems(rng, nsys=256):
+    """256 systems, N ~ U[200, 4000], half open and half single wall,
+    volume fraction ~ U[0.02, 0.25] each (a = 1): open systems uniform in a
+    cube, wall systems with x, y uniform in a square and z ~ U[1.5, 20]
+    (the slab holds the volume fraction)."""
+    sizes = rng.integers(200, 4001, nsys)
+    geoms = np.arange(nsys) % 2
+    rng.shuffle(geoms)
+    phis = rng.uniform(0.02, 0.25, nsys)
+    pos = []
+    for n, g, phi in zip(sizes, geoms, phis):
+        vol = n * 4 * math.pi / 3 / phi
+        if g:
+            L = math.sqrt(vol / 18.5)
+            pos.append(np.column_stack([rng.uniform(0, L, n), rng.uniform(0, L, n),
+                                        rng.uniform(1.5, 20, n)]))
+        else:
+            pos.append(rng.uniform(0, vol ** (1 / 3), (n, 3)))
+    return sizes, geoms, np.concatenate(pos)
+
+
+def ensemble_comparison(torch, steps, warmup, rank):
+    """Batched ensemble of 256 uneven systems (open and wall mixed) in one
+    handle, FP32, tolerance 1e-6: Mdot and sqrtMdotW for all systems per call,
+    against one NBody solver per system run one after the other."""
+    from libmobility_gb300 import NBody
+    from libmobility_gb300.ensemble import Ensemble
+    rng = np.random.default_rng(4242 + rank)
+    sizes, geoms, pos = ensemble_systems(rng)
+    ntot = int(sizes.sum())
+    eta = 1 / (6 * math.pi)
+    f32 = dict(dtype=torch.float32, device="cuda")
+    dpos = torch.tensor(pos, **f32)
+    g = torch.Generator(device="cuda").manual_seed(99 + rank)
+    dF = torch.randn(ntot, 3, generator=g, **f32)
+    dWs = [torch.randn(ntot, 3, generator=g, **f32) for _ in range(steps + warmup)]
+    e = Ensemble(precision="float")
+    e.setSystems(sizes, geoms, np.zeros(len(sizes)))
+    t0 = time.perf_counter()
+    e.initialize(viscosity=eta, hydrodynamicRadius=1.0, tolerance=1e-6, seed=5 + rank)
+    e.setPositions(dpos)
+    e.Mdot(dF)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    pairs = float(np.sum(sizes.astype(np.float64) ** 2))
+    for _ in range(3):
+        e.Mdot(dF)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    reps = 10
+    for _ in range(reps):
+        e.Mdot(dF)
+    e1.record()
+    e1.synchronize()
+    t_mdot = e0.elapsed_time(e1) * 1e-3 / reps
+    times, lat, its_all = [], [], []
+    for k, dW in enumerate(dWs):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, its, _, ms = e.sqrtMdotW(dW)
+        torch.cuda.synchronize()
+        if k >= warmup:
+            times.append(time.perf_counter() - t0)
+            lat.extend(ms.tolist())
+            its_all.append(its)
+    t_sqrt = sum(times) / len(times)
+    its_m = np.mean(its_all, axis=0)
+    sqrt_pairs = float(np.sum(sizes.astype(np.float64) ** 2 * (its_m + 1)))
+    # the same systems and noise, one NBody solver per system, one after another
+    seq = []
+    off = 0
+    dW0 = dWs[warmup]
+    for n, gm in zip(sizes, geoms):
+        s = NBody("open", "open", "single_wall" if gm else "open", precision="float")
+        s.setParameters(**({"wallHeight": 0.0} if gm else {}))
+        s.initialize(viscosity=eta, hydrodynamicRadius=1.0, tolerance=1e-6, seed=5)
+        s.setPositions(dpos[off:off + n])
+        s.sqrtMdotW_noise(dW0[off:off + n])  # first call allocates
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.sqrtMdotW_noise(dW0[off:off + n])
+        torch.cuda.synchronize()
+        seq.append(time.perf_counter() - t0)
+        off += n
+    t_seq = sum(seq)
+    return {
+        "workload": "256 systems, N ~ U[200, 4000] (total %d), half open / half single wall "
+                    "(z ~ U[1.5, 20]), phi ~ U[0.02, 0.25], FP32, tolerance 1e-6" % ntot,
+        "groups": len(e.describe()["groups"]),
+        "setup_and_autotune_s": setup_s,
+        "mdot_ms": t_mdot * 1e3,
+        "mdot_pair_interactions_per_s": pairs / t_mdot,
+        "sqrtMdotW_ms_per_call": t_sqrt * 1e3,
+        "system_solves_per_s": len(sizes) / t_sqrt,
+        "sqrtMdotW_pair_interactions_per_s": sqrt_pairs / t_sqrt,
+        "lanczos_iterations": {"min": float(np.min(its_all)), "median": float(np.median(its_all)),
+                               "max": float(np.max(its_all))},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "what": "host time from the start of the batched call until each "
+                               "system's result was known"},
+        "sequential_single_solvers_ms": t_seq * 1e3,
+        "speedup_batched_vs_sequential": t_seq / t_sqrt,
+    }
+
+
 def cpu_baseline(w, pos, F, T, seconds=8.0):
     """FP64 C oracle (all host threads) on a bounded sample of the workload:
     the first R target rows against every source."""
@@ -417,6 +523,9 @@ def run_ours(args, w, ws, rank, local):
     cmp = None
     if not args.skip_precond:
         cmp = sqrtmdotw_comparison(torch, max(2, args.steps), 2, rank)
+    ens = None
+    if not args.skip_ensemble:
+        ens = ensemble_comparison(torch, max(2, args.steps), 2, rank)
 
     if rank != 0:
         return
@@ -432,6 +541,7 @@ def run_ours(args, w, ws, rank, local):
         "sqrtMdotW": {"solves_per_s": 1.0 / t_sqrt, "lanczos_iterations": it_mean,
                       "preconditioner": "none (plain Lanczos)"},
         "sqrtMdotW_learned_vs_plain": cmp,
+        "ensemble_256": ens,
         "mdot_pair_interactions_per_s": pairs / t_mdot,
         "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
@@ -457,6 +567,8 @@ def main():
     ap.add_argument("--workload", default="wall16k", choices=sorted(WORKLOADS))
     ap.add_argument("--skip-precond", action="store_true",
                     help="skip the plain vs learned-preconditioner sqrtMdotW comparison")
+    ap.add_argument("--skip-ensemble", action="store_true",
+                    help="skip the batched ensemble of 256 uneven systems")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     ws, rank, local = dist_setup()

@@ -334,6 +334,7 @@ template <class R> class Ensemble final : public EnsembleBase {
       cudaEventDestroy(ev_t1_);
     }
     if (side_) cudaStreamDestroy(side_);
+    if (cap_) cudaStreamDestroy(cap_);
     if (own_) cudaStreamDestroy(own_);
   }
 
@@ -381,6 +382,7 @@ template <class R> class Ensemble final : public EnsembleBase {
     LMG_CUDA(cudaEventCreate(&ev_t0_));
     LMG_CUDA(cudaEventCreate(&ev_t1_));
     LMG_CUDA(cudaStreamCreateWithPriority(&side_, cudaStreamNonBlocking, -1));
+    LMG_CUDA(cudaStreamCreateWithFlags(&cap_, cudaStreamNonBlocking));
     ev_ready_ = true;
   }
   void drop_graph() {
@@ -451,11 +453,11 @@ template <class R> class Ensemble final : public EnsembleBase {
       LMG_CUDA(cudaMemsetAsync(tickets_.ptr, 0, tickets_.count * sizeof(unsigned), stream()));
     }
   }
-  void launch_group(Group &g, const R *x, R *y, const int *active) {
-    LMG_CUDA(mdot_launch<R>(shape(g), args(g, x, y, active), g.plan, stream()));
+  void launch_group(Group &g, const R *x, R *y, const int *active, cudaStream_t st) {
+    LMG_CUDA(mdot_launch<R>(shape(g), args(g, x, y, active), g.plan, st));
   }
   void matvec(const R *x, R *y, const int *active) {
-    for (auto &g : groups_) launch_group(*g, x, y, active);
+    for (auto &g : groups_) launch_group(*g, x, y, active, stream());
   }
   void ensure_plans();
   void build_graph(R *V, size_t ldv);
@@ -479,7 +481,10 @@ template <class R> class Ensemble final : public EnsembleBase {
   std::mt19937 eng_;
   std::vector<int> check_steps_;  // per internal system (registerRequiredStepsForConverge)
   // execution
-  cudaStream_t stream_ = nullptr, own_ = nullptr, side_ = nullptr;
+  // cap_ only records the per-iteration graph (the caller's stream may be
+  // the legacy default stream, which cannot be captured); the graph is then
+  // launched on the working stream
+  cudaStream_t stream_ = nullptr, own_ = nullptr, side_ = nullptr, cap_ = nullptr;
   bool have_stream_ = false, ev_ready_ = false;
   cudaEvent_t ev_iter_[2] = {nullptr, nullptr}, ev_check_ = nullptr, ev_side_ = nullptr;
   cudaEvent_t ev_t0_ = nullptr, ev_t1_ = nullptr;
@@ -669,9 +674,9 @@ template <class R> void Ensemble<R>::ensure_plans() {
       for (auto &p : plans) {
         ensure_scratch(p);
         g.plan = p;
-        launch_group(g, x, y, nullptr);  // warm-up
+        launch_group(g, x, y, nullptr, st);  // warm-up
         LMG_CUDA(cudaEventRecord(ev_t0_, st));
-        for (int r = 0; r < 3; r++) launch_group(g, x, y, nullptr);
+        for (int r = 0; r < 3; r++) launch_group(g, x, y, nullptr, st);
         LMG_CUDA(cudaEventRecord(ev_t1_, st));
         LMG_CUDA(cudaEventSynchronize(ev_t1_));
         float ms = 0;
@@ -690,22 +695,22 @@ template <class R> void Ensemble<R>::ensure_plans() {
   drop_graph();
 }
 
-// The per-iteration work captured once: every group's all-pairs launch on
-// the current basis vector (active systems only), the vector update of all
-// systems, and the iteration counter.  Re-captured whenever a buffer or plan
-// it names changes.
+// The per-iteration work captured once (on a private stream): every group's
+// all-pairs launch on the current basis vector (active systems only), the
+// vector update of all systems, and the iteration counter.  Re-captured
+// whenever a buffer or plan it names changes.
 template <class R> void Ensemble<R>::build_graph(R *V, size_t ldv) {
   const std::vector<const void *> key = {V,          w_.ptr,     vcur_.ptr,   iter_.ptr,
                                          off3_.ptr,  nn_.ptr,    active_.ptr, normz_.ptr,
                                          alpha_.ptr, beta_.ptr,  hab_.device_ptr(),
-                                         pos_.ptr,   part_.ptr,  tickets_.ptr, stream()};
+                                         pos_.ptr,   part_.ptr,  tickets_.ptr};
   if (graph_ && graph_key_ == key) return;
   drop_graph();
-  cudaStream_t st = stream();
+  cudaStream_t st = cap_;
   cudaGraph_t g = nullptr;
   LMG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   try {
-    for (auto &gp : groups_) launch_group(*gp, vcur_.ptr, w_.ptr, active_.ptr);
+    for (auto &gp : groups_) launch_group(*gp, vcur_.ptr, w_.ptr, active_.ptr, st);
     ens_step<R><<<nsys_, kEnsThreads, 0, st>>>(w_.ptr, V, vcur_.ptr, ldv, iter_.ptr,
                                                off3_.ptr, nn_.ptr, active_.ptr, normz_.ptr,
                                                alpha_.ptr, beta_.ptr, kEnsLimit,
