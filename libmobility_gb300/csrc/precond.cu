@@ -16,6 +16,7 @@ namespace lmg {
 // ---------------------------------------------------------------------------
 constexpr int kKnnThreads = 128;
 
+template <int KB>
 __global__ void __launch_bounds__(kKnnThreads)
 knn_kernel(const float *__restrict__ pos, int N, int nper, int *__restrict__ nb) {
   __shared__ float sx[kKnnThreads], sy[kKnnThreads], sz[kKnnThreads];
@@ -28,10 +29,10 @@ knn_kernel(const float *__restrict__ pos, int N, int nper, int *__restrict__ nb)
   const int last = min(N, first + kKnnThreads) - 1;
   const int s0 = (first / nper) * nper;
   const int s1 = min(N, (last / nper + 1) * nper);
-  float bd[kPrecBlocks];
-  int bj[kPrecBlocks];
+  float bd[KB];
+  int bj[KB];
 #pragma unroll
-  for (int q = 0; q < kPrecBlocks; q++) {
+  for (int q = 0; q < KB; q++) {
     bd[q] = FLT_MAX;
     bj[q] = ic;
   }
@@ -48,14 +49,14 @@ knn_kernel(const float *__restrict__ pos, int N, int nper, int *__restrict__ nb)
       const int j2 = ts + jj;
       const float dx = sx[jj] - xi, dy = sy[jj] - yi, dz = sz[jj] - zi;
       const float d = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      if (d < bd[kPrecBlocks - 1] && j2 >= b0 && j2 < b1) {
+      if (d < bd[KB - 1] && j2 >= b0 && j2 < b1) {
         // insertion into the sorted list, unrolled so it stays in registers;
         // the particle itself (d = 0) lands in slot 0
         float cd = (j2 == ic) ? -1.0f : d;
         int cj = j2;
         bool placed = false;
 #pragma unroll
-        for (int q = kPrecBlocks - 1; q >= 1; q--) {
+        for (int q = KB - 1; q >= 1; q--) {
           if (!placed) {
             if (bd[q - 1] > cd) {
               bd[q] = bd[q - 1];
@@ -77,14 +78,17 @@ knn_kernel(const float *__restrict__ pos, int N, int nper, int *__restrict__ nb)
   }
   if (i < N) {
 #pragma unroll
-    for (int q = 0; q < kPrecBlocks; q++) nb[(size_t)i * kPrecBlocks + q] = bj[q];
+    for (int q = 0; q < KB; q++) nb[(size_t)i * KB + q] = bj[q];
   }
 }
 
-cudaError_t knn_launch(const float *pos, int N, int nper, int *nb, cudaStream_t stream) {
+cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaStream_t stream) {
   const int blocks = (N + kKnnThreads - 1) / kKnnThreads;
+  if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
   count_launch();
-  knn_kernel<<<blocks, kKnnThreads, 0, stream>>>(pos, N, nper, nb);
+  if (K == 16) knn_kernel<17><<<blocks, kKnnThreads, 0, stream>>>(pos, N, nper, nb);
+  if (K == 32) knn_kernel<33><<<blocks, kKnnThreads, 0, stream>>>(pos, N, nper, nb);
+  if (K == 48) knn_kernel<49><<<blocks, kKnnThreads, 0, stream>>>(pos, N, nper, nb);
   return cudaGetLastError();
 }
 
@@ -95,16 +99,22 @@ cudaError_t knn_launch(const float *pos, int N, int nper, int *nb, cudaStream_t 
 // ---------------------------------------------------------------------------
 constexpr int kBuildThreads = 128;
 
+template <int K>
 __global__ void __launch_bounds__(kBuildThreads)
 precond_build_kernel(const float *__restrict__ pos, const int *__restrict__ nb, int N,
                      const float *__restrict__ params, float inv_a, float scale,
                      float *__restrict__ blocks) {
+  using S = PrecNet<K>;
+  constexpr int kPrecK = K, KB_ = S::Blocks, kPrecIn = S::In, kPrecHidden = S::Hidden,
+                kPrecOut = S::Out, kPrecParams = S::Params, kPrecW1 = S::W1, kPrecB1 = S::B1,
+                kPrecW2 = S::W2, kPrecB2 = S::B2, kPrecW3 = S::W3, kPrecB3 = S::B3,
+                kPrecXm = S::Xm, kPrecXs = S::Xs, kPrecYm = S::Ym, kPrecYs = S::Ys;
   extern __shared__ float sw[];
   for (int t = threadIdx.x; t < kPrecParams; t += kBuildThreads) sw[t] = params[t];
   __syncthreads();
   const int i = blockIdx.x * kBuildThreads + threadIdx.x;
   if (i >= N) return;
-  const int *nbi = nb + (size_t)i * kPrecBlocks;
+  const int *nbi = nb + (size_t)i * KB_;
   const float xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
   float rel[kPrecK][3];
 #pragma unroll
@@ -174,7 +184,7 @@ precond_build_kernel(const float *__restrict__ pos, const int *__restrict__ nb, 
       acc = fmaf(h1[k], sw[kPrecW2 + k * kPrecHidden + j], acc);
     h2[j] = tanhf(acc);
   }
-  float *out = blocks + (size_t)i * kPrecBlocks * 9;
+  float *out = blocks + (size_t)i * KB_ * 9;
   // output unit o, de-normalised
   auto unit = [&](int o) {
     float acc = sw[kPrecB3 + o];
@@ -183,7 +193,7 @@ precond_build_kernel(const float *__restrict__ pos, const int *__restrict__ nb, 
     return acc * sw[kPrecYs + o] + sw[kPrecYm + o];
   };
 #pragma unroll 1
-  for (int n = 0; n < kPrecBlocks; n++) {
+  for (int n = 0; n < KB_; n++) {
     float b[3][3];
     if (n == 0) {  // symmetric self block from 6 units: 00 01 02 11 12 22
       const float u0 = unit(0), u1 = unit(1), u2 = unit(2), u3 = unit(3), u4 = unit(4),
@@ -215,31 +225,42 @@ precond_build_kernel(const float *__restrict__ pos, const int *__restrict__ nb, 
   }
 }
 
-cudaError_t precond_build_launch(const float *pos, const int *nb, int N, const float *params,
-                                 float inv_a, float scale, float *blocks, cudaStream_t stream) {
-  const size_t smem = kPrecParams * sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(precond_build_kernel,
+template <int K>
+cudaError_t precond_build_k(const float *pos, const int *nb, int N, const float *params,
+                            float inv_a, float scale, float *blocks, cudaStream_t stream) {
+  const size_t smem = PrecNet<K>::Params * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(precond_build_kernel<K>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int nblk = (N + kBuildThreads - 1) / kBuildThreads;
   count_launch();
-  precond_build_kernel<<<nblk, kBuildThreads, smem, stream>>>(pos, nb, N, params, inv_a, scale,
-                                                              blocks);
+  precond_build_kernel<K><<<nblk, kBuildThreads, smem, stream>>>(pos, nb, N, params, inv_a,
+                                                                 scale, blocks);
   return cudaGetLastError();
 }
 
+cudaError_t precond_build_launch(int K, const float *pos, const int *nb, int N,
+                                 const float *params, float inv_a, float scale, float *blocks,
+                                 cudaStream_t stream) {
+  if (K == 16) return precond_build_k<16>(pos, nb, N, params, inv_a, scale, blocks, stream);
+  if (K == 32) return precond_build_k<32>(pos, nb, N, params, inv_a, scale, blocks, stream);
+  if (K == 48) return precond_build_k<48>(pos, nb, N, params, inv_a, scale, blocks, stream);
+  return cudaErrorInvalidValue;
+}
+
 // ---------------------------------------------------------------------------
-// Sparse products with P (rows of 17 3x3 blocks)
+// Sparse products with P (rows of K+1 3x3 blocks)
 // ---------------------------------------------------------------------------
+template <int KB>
 __global__ void precond_apply_kernel(const float *__restrict__ B, const int *__restrict__ nb,
                                      int N, const float *__restrict__ x, float *__restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  const float *b = B + (size_t)i * kPrecBlocks * 9;
-  const int *nbi = nb + (size_t)i * kPrecBlocks;
+  const float *b = B + (size_t)i * KB * 9;
+  const int *nbi = nb + (size_t)i * KB;
   float o0 = 0.f, o1 = 0.f, o2 = 0.f;
 #pragma unroll
-  for (int n = 0; n < kPrecBlocks; n++) {
+  for (int n = 0; n < KB; n++) {
     const int j = nbi[n];
     const float v0 = x[3 * j], v1 = x[3 * j + 1], v2 = x[3 * j + 2];
     o0 = fmaf(b[9 * n + 0], v0, fmaf(b[9 * n + 1], v1, fmaf(b[9 * n + 2], v2, o0)));
@@ -251,15 +272,16 @@ __global__ void precond_apply_kernel(const float *__restrict__ B, const int *__r
   out[3 * i + 2] = o2;
 }
 
+template <int KB>
 __global__ void precond_apply_t_kernel(const float *__restrict__ B, const int *__restrict__ nb,
                                        int N, const float *__restrict__ x, float *out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  const float *b = B + (size_t)i * kPrecBlocks * 9;
-  const int *nbi = nb + (size_t)i * kPrecBlocks;
+  const float *b = B + (size_t)i * KB * 9;
+  const int *nbi = nb + (size_t)i * KB;
   const float v0 = x[3 * i], v1 = x[3 * i + 1], v2 = x[3 * i + 2];
 #pragma unroll
-  for (int n = 0; n < kPrecBlocks; n++) {
+  for (int n = 0; n < KB; n++) {
     const int j = nbi[n];
     atomicAdd(out + 3 * j, b[9 * n + 0] * v0 + b[9 * n + 3] * v1 + b[9 * n + 6] * v2);
     atomicAdd(out + 3 * j + 1, b[9 * n + 1] * v0 + b[9 * n + 4] * v1 + b[9 * n + 7] * v2);
@@ -267,17 +289,25 @@ __global__ void precond_apply_t_kernel(const float *__restrict__ B, const int *_
   }
 }
 
-cudaError_t precond_apply_launch(const float *blocks, const int *nb, int N, const float *x,
-                                 float *out, cudaStream_t stream) {
+cudaError_t precond_apply_launch(int K, const float *blocks, const int *nb, int N,
+                                 const float *x, float *out, cudaStream_t stream) {
+  const int g = (N + 255) / 256;
+  if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
   count_launch();
-  precond_apply_kernel<<<(N + 255) / 256, 256, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 16) precond_apply_kernel<17><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 32) precond_apply_kernel<33><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 48) precond_apply_kernel<49><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
   return cudaGetLastError();
 }
 
-cudaError_t precond_apply_t_launch(const float *blocks, const int *nb, int N, const float *x,
-                                   float *out, cudaStream_t stream) {
+cudaError_t precond_apply_t_launch(int K, const float *blocks, const int *nb, int N,
+                                   const float *x, float *out, cudaStream_t stream) {
+  const int g = (N + 255) / 256;
+  if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
   count_launch();
-  precond_apply_t_kernel<<<(N + 255) / 256, 256, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 16) precond_apply_t_kernel<17><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 32) precond_apply_t_kernel<33><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 48) precond_apply_t_kernel<49><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
   return cudaGetLastError();
 }
 
@@ -438,22 +468,39 @@ int lmg_internal_adam(size_t n, float *w, const float *g, float *m, float *v, fl
   return (int)cudaGetLastError();
 }
 
+int lmg_internal_knn_k(int K, const float *pos, int N, int nper, int *nb, void *stream) {
+  return (int)knn_launch(K, pos, N, nper, nb, (cudaStream_t)stream);
+}
+
+int lmg_internal_precond_build_k(int K, const float *pos, const int *nb, int N,
+                                 const float *params, float inv_a, float scale, float *blocks,
+                                 void *stream) {
+  return (int)precond_build_launch(K, pos, nb, N, params, inv_a, scale, blocks,
+                                   (cudaStream_t)stream);
+}
+
+int lmg_internal_precond_apply_k(int K, const float *blocks, const int *nb, int N,
+                                 const float *x, float *out, int transpose, void *stream) {
+  if (transpose) {
+    cudaMemsetAsync(out, 0, 3 * (size_t)N * sizeof(float), (cudaStream_t)stream);
+    return (int)precond_apply_t_launch(K, blocks, nb, N, x, out, (cudaStream_t)stream);
+  }
+  return (int)precond_apply_launch(K, blocks, nb, N, x, out, (cudaStream_t)stream);
+}
+
+// K = 16 forms
 int lmg_internal_knn(const float *pos, int N, int nper, int *nb, void *stream) {
-  return (int)knn_launch(pos, N, nper, nb, (cudaStream_t)stream);
+  return lmg_internal_knn_k(16, pos, N, nper, nb, stream);
 }
 
 int lmg_internal_precond_build(const float *pos, const int *nb, int N, const float *params,
                                float inv_a, float scale, float *blocks, void *stream) {
-  return (int)precond_build_launch(pos, nb, N, params, inv_a, scale, blocks, (cudaStream_t)stream);
+  return lmg_internal_precond_build_k(16, pos, nb, N, params, inv_a, scale, blocks, stream);
 }
 
 int lmg_internal_precond_apply(const float *blocks, const int *nb, int N, const float *x,
                                float *out, int transpose, void *stream) {
-  if (transpose) {
-    cudaMemsetAsync(out, 0, 3 * (size_t)N * sizeof(float), (cudaStream_t)stream);
-    return (int)precond_apply_t_launch(blocks, nb, N, x, out, (cudaStream_t)stream);
-  }
-  return (int)precond_apply_launch(blocks, nb, N, x, out, (cudaStream_t)stream);
+  return lmg_internal_precond_apply_k(16, blocks, nb, N, x, out, transpose, stream);
 }
 
 }  // extern "C"

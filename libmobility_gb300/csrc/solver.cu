@@ -139,6 +139,7 @@ template <class R> class Solver final : public SolverBase {
   // learned preconditioner
   bool prec_on_ = false;
   bool prec_dirty_ = true;
+  int prec_k_ = 16;  // neighbours per row of P, from the network's parameter count
   DeviceBuffer<float> prec_params_, prec_blocks_;
   DeviceBuffer<int> prec_nb_;
   DeviceBuffer<R> pt_, pu_, bx_, br_, brh_, bp_, bv_, bs_, bt_;  // operator and BiCGSTAB vectors
@@ -682,12 +683,16 @@ void Solver<R>::set_preconditioner(const std::string &kind, const float *params,
   if (!std::is_same<R, float>::value)
     throw Error(LMG_ERR_INVALID_ARGUMENT,
                 "[libmobility_gb300] the learned preconditioner needs precision float");
-  if (!params || n != (size_t)kPrecParams)
+  const int k = params ? prec_k_for_params(n) : 0;
+  if (k == 0)
     throw Error(LMG_ERR_INVALID_ARGUMENT,
                 "[libmobility_gb300] preconditioner parameters must hold " +
-                    std::to_string(kPrecParams) + " floats");
-  float *d = prec_params_.ensure(kPrecParams);
-  LMG_CUDA(cudaMemcpy(d, params, kPrecParams * sizeof(float), cudaMemcpyHostToDevice));
+                    std::to_string(PrecNet<16>::Params) + ", " +
+                    std::to_string(PrecNet<32>::Params) + " or " +
+                    std::to_string(PrecNet<48>::Params) + " floats (K = 16, 32, 48)");
+  float *d = prec_params_.ensure(n);
+  LMG_CUDA(cudaMemcpy(d, params, n * sizeof(float), cudaMemcpyHostToDevice));
+  prec_k_ = k;
   prec_on_ = true;
   prec_dirty_ = true;
 }
@@ -695,18 +700,19 @@ void Solver<R>::set_preconditioner(const std::string &kind, const float *params,
 // The preconditioner needs at least K + 1 particles per batch; smaller
 // systems fall back to plain Lanczos.
 template <class R> bool Solver<R>::prec_active() const {
-  return prec_on_ && std::is_same<R, float>::value && batch_size() >= kPrecK + 1;
+  return prec_on_ && std::is_same<R, float>::value && batch_size() >= prec_k_ + 1;
 }
 
 template <class R> void Solver<R>::prec_build() {
   if constexpr (std::is_same<R, float>::value) {
     if (!prec_dirty_) return;
     const int N = (int)N_;
-    int *nb = prec_nb_.ensure((size_t)N * kPrecBlocks);
-    float *blocks = prec_blocks_.ensure((size_t)N * kPrecBlocks * 9);
-    LMG_CUDA(knn_launch(pos_.ptr, N, batch_size(), nb, stream()));
+    const int kb = prec_k_ + 1;
+    int *nb = prec_nb_.ensure((size_t)N * kb);
+    float *blocks = prec_blocks_.ensure((size_t)N * kb * 9);
+    LMG_CUDA(knn_launch(prec_k_, pos_.ptr, N, batch_size(), nb, stream()));
     // targets were trained with t0 = 1: M^{-1/2} scales as t0^{-1/2}
-    LMG_CUDA(precond_build_launch(pos_.ptr, nb, N, prec_params_.ptr, (float)(1.0 / a_),
+    LMG_CUDA(precond_build_launch(prec_k_, pos_.ptr, nb, N, prec_params_.ptr, (float)(1.0 / a_),
                                   (float)(1.0 / std::sqrt(t0_)), blocks, stream()));
     prec_dirty_ = false;
   }
@@ -725,13 +731,13 @@ template <class R> void Solver<R>::apply_operator(const R *v, R *out) {
     R *u = pu_.ensure(n);
     const R s = (R)(1.0 / std::sqrt(r0_));  // angular part: scalar r0^{-1/2}
     LMG_CUDA(cudaMemsetAsync(t, 0, n3 * sizeof(R), stream()));
-    LMG_CUDA(precond_apply_t_launch(prec_blocks_.ptr, prec_nb_.ptr, N, v, t, stream()));
+    LMG_CUDA(precond_apply_t_launch(prec_k_, prec_blocks_.ptr, prec_nb_.ptr, N, v, t, stream()));
     if (ang_) {
       scale_kernel<R><<<vec_blocks(n3), kRedThreads, 0, stream()>>>(t + n3, v + n3, n3, s);
       count_launch();
     }
     mdot_device(pos_.ptr, t, ang_ ? t + n3 : nullptr, u, ang_ ? u + n3 : nullptr);
-    LMG_CUDA(precond_apply_launch(prec_blocks_.ptr, prec_nb_.ptr, N, u, out, stream()));
+    LMG_CUDA(precond_apply_launch(prec_k_, prec_blocks_.ptr, prec_nb_.ptr, N, u, out, stream()));
     if (ang_) {
       scale_kernel<R><<<vec_blocks(n3), kRedThreads, 0, stream()>>>(out + n3, u + n3, n3, s);
       count_launch();
@@ -779,7 +785,7 @@ template <class R> int Solver<R>::solve_p(const R *b, R *x) {
       bicg_p_kernel<R><<<blocks, kRedThreads, 0, st>>>(p, r, v, it == 1 ? 0.0 : beta,
                                                        omega, n);
       count_launch();
-      LMG_CUDA(precond_apply_launch(prec_blocks_.ptr, prec_nb_.ptr, N, p, v, st));
+      LMG_CUDA(precond_apply_launch(prec_k_, prec_blocks_.ptr, prec_nb_.ptr, N, p, v, st));
       dot2_kernel<R><<<blocks, kRedThreads, 0, st>>>(rh, v, rh, v, n, rp, tk, out);
       count_launch();
       sync();
@@ -797,7 +803,7 @@ template <class R> int Solver<R>::solve_p(const R *b, R *x) {
         sync();
         return it;
       }
-      LMG_CUDA(precond_apply_launch(prec_blocks_.ptr, prec_nb_.ptr, N, s, t, st));
+      LMG_CUDA(precond_apply_launch(prec_k_, prec_blocks_.ptr, prec_nb_.ptr, N, s, t, st));
       dot2_kernel<R><<<blocks, kRedThreads, 0, st>>>(t, s, t, t, n, rp, tk, out);
       count_launch();
       sync();

@@ -4,15 +4,16 @@ csrc/precond.cuh for what P is and why it is sparse).
 Training data are made by the method itself: random small particle systems
 (N uniform in 64..512, volume fraction uniform in 0.05..0.3, half of them as
 Gaussian clusters of ~128 particles with sigma = 4a, overlaps at 2a removed);
-for sampled particles the 17-particle neighbourhood mobility (open-boundary RPY,
-t0 = 1, a = 1) is inverted-square-rooted exactly in FP64 (dense eigh) and its
-first block row, rotated into the particle's canonical frame, is the target.
+for sampled particles the (K+1)-particle neighbourhood mobility (open-boundary
+RPY, t0 = 1, a = 1; K = 16, 32 or 48 nearest neighbours) is inverted-square-
+rooted exactly in FP64 (dense eigh) and its first block row, rotated into the
+particle's canonical frame, is the target.
 
 The network is trained on the GPU by this project's own kernels
 (lmg_internal_gemm / _tanh_backward / _mse_grad / _colsum / _adam in
 csrc/precond.cu); PyTorch only provides device memory.
 
-    python -m libmobility_gb300.precond train --systems 20000 --out weights.npz
+    python -m libmobility_gb300.precond train --k 48 --systems 20000 --out weights.npz
 """
 import argparse
 import ctypes
@@ -25,10 +26,23 @@ from pathlib import Path
 
 import numpy as np
 
-K = 16
-NIN, NH, NOUT = 3 * K, 64, 6 + 9 * K
+NH = 64
 WEIGHTS_DIR = Path(__file__).resolve().parent / "weights"
-DEFAULT_WEIGHTS = WEIGHTS_DIR / "precond_open_k16.npz"
+
+
+def weights_path(k):
+    return WEIGHTS_DIR / f"precond_open_k{k}.npz"
+
+
+def _default_weights():
+    """The shipped network with the most neighbours."""
+    for k in (48, 32, 16):
+        if weights_path(k).exists():
+            return weights_path(k)
+    return weights_path(16)
+
+
+DEFAULT_WEIGHTS = _default_weights()
 SYM = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
 
 
@@ -114,7 +128,7 @@ def canonical_frames(rel):
     ex = rel[:, 0] / np.linalg.norm(rel[:, 0], axis=1, keepdims=True)
     ey = np.zeros_like(ex)
     done = np.zeros(B, bool)
-    for n in range(1, K):
+    for n in range(1, rel.shape[1]):
         a = rel[:, n] - ex * np.sum(rel[:, n] * ex, axis=1, keepdims=True)
         nn = np.sum(a * a, axis=1)
         take = (~done) & (nn > 1e-12)
@@ -125,19 +139,19 @@ def canonical_frames(rel):
     return np.stack([ex, ey, ez], axis=1)
 
 
-def samples_from_system(p, ids):
-    """Features X (B, 48) and targets Y (B, 150) for particles `ids` of p."""
+def samples_from_system(p, ids, K=16):
+    """Features X (B, 3K) and targets Y (B, 6 + 9K) for particles `ids` of p."""
     from scipy.spatial import cKDTree
     _, nb = cKDTree(p).query(p[ids], K + 1)
     rel = p[nb[:, 1:]] - p[ids][:, None, :]
     E = canonical_frames(rel)
     X = np.einsum("bnk,bck->bnc", rel, E).reshape(len(ids), -1)
-    P = p[nb]                                                   # B, 17, 3
-    blocks = rpy_uf_blocks(P[:, :, None, :] - P[:, None, :, :])  # B,17,17,3,3
+    P = p[nb]                                                   # B, K+1, 3
+    blocks = rpy_uf_blocks(P[:, :, None, :] - P[:, None, :, :])  # B,K+1,K+1,3,3
     Mp = blocks.transpose(0, 1, 3, 2, 4).reshape(len(ids), 3 * (K + 1), 3 * (K + 1))
     lam, Q = np.linalg.eigh(Mp)
-    row = np.einsum("bij,bj,bkj->bik", Q[:, :3, :], 1.0 / np.sqrt(lam), Q)  # B,3,51
-    rb = row.reshape(len(ids), 3, K + 1, 3).transpose(0, 2, 1, 3)         # B,17,3,3
+    row = np.einsum("bij,bj,bkj->bik", Q[:, :3, :], 1.0 / np.sqrt(lam), Q)  # B,3,3(K+1)
+    rb = row.reshape(len(ids), 3, K + 1, 3).transpose(0, 2, 1, 3)         # B,K+1,3,3
     rc = np.einsum("bij,bnjk,blk->bnil", E, rb, E)                         # canonical frame
     Y = np.concatenate([np.stack([rc[:, 0, i, j] for i, j in SYM], 1),
                         rc[:, 1:].reshape(len(ids), -1)], 1)
@@ -145,7 +159,7 @@ def samples_from_system(p, ids):
 
 
 def _make_chunk(args):
-    seed, nsys, per_sys = args
+    seed, nsys, per_sys, k = args
     rng = np.random.default_rng(seed)
     Xs, Ys = [], []
     for _ in range(nsys):
@@ -153,13 +167,13 @@ def _make_chunk(args):
         phi = float(rng.uniform(0.05, 0.3))
         p = random_system(rng, n, phi, rng.random() < 0.5)
         ids = rng.choice(n, min(n, per_sys), replace=False)
-        X, Y = samples_from_system(p, ids)
+        X, Y = samples_from_system(p, ids, k)
         Xs.append(X)
         Ys.append(Y)
     return np.concatenate(Xs), np.concatenate(Ys)
 
 
-def make_dataset(systems, per_sys=32, seed=0, workers=None, log=None):
+def make_dataset(systems, per_sys=32, seed=0, workers=None, log=None, k=16):
     workers = workers or max(1, (os.cpu_count() or 1))
     # one BLAS thread per worker: the pool already uses every core
     for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
@@ -168,7 +182,7 @@ def make_dataset(systems, per_sys=32, seed=0, workers=None, log=None):
     jobs = []
     s = 0
     while s < systems:
-        jobs.append((seed * 1000003 + len(jobs), min(chunk, systems - s), per_sys))
+        jobs.append((seed * 1000003 + len(jobs), min(chunk, systems - s), per_sys, k))
         s += chunk
     ctx = mp.get_context("spawn")
     parts = []
@@ -184,14 +198,32 @@ def make_dataset(systems, per_sys=32, seed=0, workers=None, log=None):
 # ---------------------------------------------------------------------------
 # parameters
 # ---------------------------------------------------------------------------
-LAYOUT = [("W1", (NIN, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)),
-          ("W3", (NH, NOUT)), ("b3", (NOUT,)), ("xmean", (NIN,)), ("xstd", (NIN,)),
-          ("ymean", (NOUT,)), ("ystd", (NOUT,))]
-NTRAIN = NIN * NH + NH + NH * NH + NH + NH * NOUT + NOUT  # trainable prefix
+def layout(k):
+    """Parameter layout for k neighbours, as csrc/precond.cuh (PrecNet<K>)."""
+    nin, nout = 3 * k, 6 + 9 * k
+    return [("W1", (nin, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)),
+            ("W3", (NH, nout)), ("b3", (nout,)), ("xmean", (nin,)), ("xstd", (nin,)),
+            ("ymean", (nout,)), ("ystd", (nout,))]
+
+
+def ntrain(k):
+    """Length of the trainable prefix (weights and biases)."""
+    nin, nout = 3 * k, 6 + 9 * k
+    return nin * NH + NH + NH * NH + NH + NH * nout + nout
+
+
+def k_of_params(n):
+    for k in (16, 32, 48):
+        if n == sum(int(np.prod(s)) for _, s in layout(k)):
+            return k
+    raise ValueError(f"{n} is not the parameter count of a K = 16, 32 or 48 network")
+
+
+LAYOUT = layout(16)
 
 
 def flat_params(d):
-    return np.concatenate([np.asarray(d[k], np.float32).ravel() for k, _ in LAYOUT])
+    return np.concatenate([np.asarray(d[name], np.float32).ravel() for name, _ in LAYOUT])
 
 
 def load_weights(path=None):
@@ -209,19 +241,21 @@ def load_weights(path=None):
 class GpuMLP:
     def __init__(self, lib, torch, params, stream):
         self.lib, self.torch, self.s = lib, torch, stream
+        self.k = k_of_params(len(params))
+        self.nin, self.nout, self.ntrain = 3 * self.k, 6 + 9 * self.k, ntrain(self.k)
         self.p = torch.tensor(params, device="cuda")
-        self.g = torch.zeros(NTRAIN, device="cuda")
-        self.m = torch.zeros(NTRAIN, device="cuda")
-        self.v = torch.zeros(NTRAIN, device="cuda")
+        self.g = torch.zeros(self.ntrain, device="cuda")
+        self.m = torch.zeros(self.ntrain, device="cuda")
+        self.v = torch.zeros(self.ntrain, device="cuda")
         self.loss = torch.zeros(1, dtype=torch.float64, device="cuda")
         off = 0
         self.view = {}
         self.gview = {}
-        for k, shp in LAYOUT:
+        for name, shp in layout(self.k):
             n = int(np.prod(shp))
-            self.view[k] = self.p[off:off + n]
-            if off < NTRAIN:
-                self.gview[k] = self.g[off:off + n]
+            self.view[name] = self.p[off:off + n]
+            if off < self.ntrain:
+                self.gview[name] = self.g[off:off + n]
             off += n
 
     def _ptr(self, t):
@@ -237,6 +271,7 @@ class GpuMLP:
     def forward(self, X, H1, H2, Yp):
         B = X.shape[0]
         v = self.view
+        NIN, NOUT = self.nin, self.nout
         self.gemm(0, 0, B, NH, NIN, X, NIN, v["W1"], NH, H1, NH, v["b1"], 1)
         self.gemm(0, 0, B, NH, NH, H1, NH, v["W2"], NH, H2, NH, v["b2"], 1)
         self.gemm(0, 0, B, NOUT, NH, H2, NH, v["W3"], NOUT, Yp, NOUT, v["b3"], 0)
@@ -244,6 +279,7 @@ class GpuMLP:
     def backward(self, X, H1, H2, Yp, T, dY, dH2, dH1):
         B = X.shape[0]
         v, g, lib = self.view, self.gview, self.lib
+        NIN, NOUT = self.nin, self.nout
         scale = ctypes.c_float(2.0 / (B * NOUT))
         assert lib.lmg_internal_mse_grad(ctypes.c_size_t(B * NOUT), self._ptr(Yp), self._ptr(T),
                                          self._ptr(dY), scale, self._ptr(self.loss), self.s) == 0
@@ -261,7 +297,7 @@ class GpuMLP:
         assert lib.lmg_internal_colsum(B, NH, self._ptr(dH1), self._ptr(g["b1"]), self.s) == 0
 
     def adam(self, lr, step):
-        assert self.lib.lmg_internal_adam(ctypes.c_size_t(NTRAIN), self._ptr(self.p),
+        assert self.lib.lmg_internal_adam(ctypes.c_size_t(self.ntrain), self._ptr(self.p),
                                           self._ptr(self.g), self._ptr(self.m), self._ptr(self.v),
                                           ctypes.c_float(lr), ctypes.c_float(0.9),
                                           ctypes.c_float(0.999), ctypes.c_float(1e-8), step,
@@ -270,6 +306,7 @@ class GpuMLP:
 
 def init_params(X, Y, seed=0):
     rng = np.random.default_rng(seed)
+    NIN, NOUT = X.shape[1], Y.shape[1]
     d = {}
     d["W1"] = rng.normal(0, 1 / math.sqrt(NIN), (NIN, NH))
     d["b1"] = np.zeros(NH)
@@ -287,7 +324,9 @@ def train(X, Y, epochs=60, batch=4096, lr=2e-3, seed=0, log=print, val_frac=0.05
     from . import _capi
     lib = _capi.load()
     d = init_params(X, Y, seed)
-    params = flat_params(d)
+    k = X.shape[1] // 3
+    NIN, NOUT = 3 * k, 6 + 9 * k
+    params = np.concatenate([np.asarray(d[name], np.float32).ravel() for name, _ in layout(k)])
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     net = GpuMLP(lib, torch, params, stream)
     xm, xs = d["xmean"].astype(np.float32), d["xstd"].astype(np.float32)
@@ -327,7 +366,7 @@ def train(X, Y, epochs=60, batch=4096, lr=2e-3, seed=0, log=print, val_frac=0.05
         hist.append((ep, train_mse, val))
         if ep % 5 == 0 or ep == epochs - 1:
             log(f"epoch {ep:3d} train mse {train_mse:.4f} val mse {val:.4f} ({time.time()-t0:.1f}s)")
-    out = {k: net.view[k].detach().cpu().numpy().reshape(shp) for k, shp in LAYOUT}
+    out = {name: net.view[name].detach().cpu().numpy().reshape(shp) for name, shp in layout(k)}
     out["xmean"], out["xstd"], out["ymean"], out["ystd"] = xm, xs, ym, ys
     return out, hist
 
@@ -339,33 +378,36 @@ def evaluate(net, Xv, Yv, batch, torch):
         B = xb.shape[0]
         H1 = torch.empty(B, NH, device="cuda")
         H2 = torch.empty_like(H1)
-        Yp = torch.empty(B, NOUT, device="cuda")
+        Yp = torch.empty(B, net.nout, device="cuda")
         net.forward(xb, H1, H2, Yp)
         tot += float(((Yp - Yv[b0:b0 + B]) ** 2).sum())
-    return tot / (Xv.shape[0] * NOUT)
+    return tot / (Xv.shape[0] * net.nout)
 
 
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd")
     t = sub.add_parser("train")
+    t.add_argument("--k", type=int, default=16, choices=[16, 32, 48])
     t.add_argument("--systems", type=int, default=20000)
     t.add_argument("--per-system", type=int, default=32)
     t.add_argument("--epochs", type=int, default=60)
-    t.add_argument("--out", default=str(DEFAULT_WEIGHTS))
+    t.add_argument("--out", default=None)
     t.add_argument("--seed", type=int, default=0)
     a = ap.parse_args()
     if a.cmd == "train":
         t0 = time.time()
         X, Y = make_dataset(a.systems, a.per_system, a.seed,
-                            log=lambda m: print(m, flush=True))
+                            log=lambda m: print(m, flush=True), k=a.k)
         print(f"dataset {X.shape} {Y.shape} in {time.time()-t0:.1f}s", flush=True)
         w, hist = train(X, Y, epochs=a.epochs, seed=a.seed)
-        Path(a.out).parent.mkdir(parents=True, exist_ok=True)
-        np.savez(a.out, **w, history=np.array(hist),
+        out = a.out or str(weights_path(a.k))
+        Path(out).parent.mkdir(parents=True, exist_ok=True)
+        np.savez(out, **w, history=np.array(hist),
                  info=np.array(json.dumps({"systems": a.systems, "per_system": a.per_system,
-                                           "epochs": a.epochs, "samples": int(X.shape[0])})))
-        print("saved", a.out)
+                                           "epochs": a.epochs, "samples": int(X.shape[0]),
+                                           "k": a.k})))
+        print("saved", out)
 
 
 if __name__ == "__main__":

@@ -8,15 +8,33 @@ scipy's k-d tree, the canonical frame, the MLP forward and backward passes
 import numpy as np
 
 K = 16
-NIN, NH, NOUT = 48, 64, 150
-SHAPES = [("W1", (NIN, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)),
-          ("W3", (NH, NOUT)), ("b3", (NOUT,)), ("xmean", (NIN,)), ("xstd", (NIN,)),
-          ("ymean", (NOUT,)), ("ystd", (NOUT,))]
+NH = 64
+
+
+def shapes(k=K):
+    """Parameter layout of the network for k neighbours (3k -> 64 -> 64 ->
+    6 + 9k)."""
+    nin, nout = 3 * k, 6 + 9 * k
+    return [("W1", (nin, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)),
+            ("W3", (NH, nout)), ("b3", (nout,)), ("xmean", (nin,)), ("xstd", (nin,)),
+            ("ymean", (nout,)), ("ystd", (nout,))]
+
+
+SHAPES = shapes(K)
+NIN, NOUT = 3 * K, 6 + 9 * K
+
+
+def k_of(flat):
+    """Neighbour count of a flat parameter vector."""
+    for k in (16, 32, 48):
+        if len(flat) == sum(int(np.prod(s)) for _, s in shapes(k)):
+            return k
+    raise ValueError("not a preconditioner parameter vector")
 
 
 def unpack(flat):
     out, o = {}, 0
-    for k, shp in SHAPES:
+    for k, shp in shapes(k_of(flat)):
         n = int(np.prod(shp))
         out[k] = np.asarray(flat[o:o + n], np.float64).reshape(shp)
         o += n
@@ -24,7 +42,7 @@ def unpack(flat):
 
 
 def pack(d):
-    return np.concatenate([np.asarray(d[k], np.float32).ravel() for k, _ in SHAPES])
+    return np.concatenate([np.asarray(d[name], np.float32).ravel() for name, _ in SHAPES])
 
 
 def neighbours(pos, k=K):
@@ -65,9 +83,10 @@ def backward(d, X, H1, H2, Y, T):
 
 
 def p_blocks(pos, flat, a=1.0, scale=1.0):
-    """Lab-frame blocks (N, 17, 3, 3) and neighbour lists (N, 17)."""
+    """Lab-frame blocks (N, K+1, 3, 3) and neighbour lists (N, K+1)."""
     d = unpack(flat)
-    nb, _ = neighbours(pos)
+    K = k_of(flat)
+    nb, _ = neighbours(pos, K)
     N = pos.shape[0]
     out = np.zeros((N, K + 1, 3, 3))
     for i in range(N):
@@ -87,16 +106,16 @@ def dense_p(blocks, nb):
     N = blocks.shape[0]
     P = np.zeros((3 * N, 3 * N))
     for i in range(N):
-        for n in range(K + 1):
+        for n in range(nb.shape[1]):
             j = nb[i, n]
             P[3 * i:3 * i + 3, 3 * j:3 * j + 3] += blocks[i, n]
     return P
 
 
-def identity_params():
+def identity_params(k=K):
     """A network whose output is the identity self block and zero neighbour
     blocks for every input (all weights zero, output mean = identity)."""
-    d = {k: np.zeros(shp) for k, shp in SHAPES}
+    d = {name: np.zeros(shp) for name, shp in shapes(k)}
     d["xstd"][:] = 1.0
     d["ystd"][:] = 1.0
     d["ymean"][[0, 3, 5]] = 1.0

@@ -107,6 +107,52 @@ def test_build_and_apply_match_oracle(cuda, po):
         assert np.allclose(out.cpu().numpy(), ref_y, rtol=1e-4, atol=1e-5 * np.abs(ref_y).max())
 
 
+@pytest.mark.parametrize("K", [32, 48])
+def test_wider_networks_match_oracle(cuda, po, K):
+    """kNN, P build and P / P^T products for networks over K = 32 and 48
+    neighbours, against the NumPy oracle."""
+    import torch
+    lib = _lib()
+    rng = np.random.default_rng(K)
+    N = 200
+    p = _clustered(rng, N).astype(np.float32)
+    d = {k: rng.normal(0, 0.3, shp) for k, shp in po.shapes(K)}
+    d["xstd"] = np.abs(d["xstd"]) + 1.0
+    d["ystd"] = np.abs(d["ystd"]) + 0.5
+    params = np.concatenate([np.asarray(d[k], np.float32).ravel() for k, _ in po.shapes(K)])
+    dp = torch.tensor(p, device="cuda")
+    nb = torch.empty((N, K + 1), dtype=torch.int32, device="cuda")
+    blocks = torch.empty((N, K + 1, 9), dtype=torch.float32, device="cuda")
+    dparams = torch.tensor(params, device="cuda")
+    assert lib.lmg_internal_knn_k(K, ctypes.c_void_p(dp.data_ptr()), N, N,
+                                  ctypes.c_void_p(nb.data_ptr()), None) == 0
+    a, scale = 1.3, 0.7
+    assert lib.lmg_internal_precond_build_k(K, ctypes.c_void_p(dp.data_ptr()),
+                                            ctypes.c_void_p(nb.data_ptr()), N,
+                                            ctypes.c_void_p(dparams.data_ptr()), 1.0 / a, scale,
+                                            ctypes.c_void_p(blocks.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    ref, nb_ref = po.p_blocks(p.astype(np.float64), params, a=a, scale=scale)
+    got = blocks.cpu().numpy().reshape(N, K + 1, 3, 3)
+    nbg = nb.cpu().numpy()
+    for i in range(N):
+        assert set(nbg[i]) == set(nb_ref[i])
+        m = {int(j): got[i, n] for n, j in enumerate(nbg[i])}
+        for n, j in enumerate(nb_ref[i]):
+            assert np.allclose(m[int(j)], ref[i, n], rtol=2e-3, atol=2e-4 * np.abs(ref[i]).max())
+    P = po.dense_p(got.astype(np.float64), nbg)
+    x = rng.normal(size=3 * N).astype(np.float32)
+    dx = torch.tensor(x, device="cuda")
+    out = torch.empty(3 * N, device="cuda")
+    for tr, ref_y in ((0, P @ x), (1, P.T @ x)):
+        assert lib.lmg_internal_precond_apply_k(K, ctypes.c_void_p(blocks.data_ptr()),
+                                                ctypes.c_void_p(nb.data_ptr()), N,
+                                                ctypes.c_void_p(dx.data_ptr()),
+                                                ctypes.c_void_p(out.data_ptr()), tr, None) == 0
+        torch.cuda.synchronize()
+        assert np.allclose(out.cpu().numpy(), ref_y, rtol=1e-4, atol=1e-5 * np.abs(ref_y).max())
+
+
 def test_training_kernels_gradient_check(cuda, po):
     """Forward pass and gradients of the project's GEMM/tanh/MSE/colsum
     kernels against the NumPy oracle."""
