@@ -370,6 +370,40 @@ def ensemble_comparison(torch, steps, warmup, rank):
     }
 
 
+def large_wall_mdot(torch, rank, reps=3):
+    """Configuration 5's matrix-vector product: single wall, N = 262144,
+    x, y ~ U[0, 1024), z ~ U[1.5, 40], forces and torques, includeAngular,
+    FP32; CUDA events around `reps` launches on device-resident inputs (its
+    FP64 check on 4096 rows is tests/test_large_gpu.py)."""
+    from libmobility_gb300 import NBody
+    N = 262144
+    rng = np.random.default_rng(31 + rank)
+    pos = np.column_stack([rng.uniform(0, 1024, N), rng.uniform(0, 1024, N),
+                           rng.uniform(1.5, 40, N)])
+    f32 = dict(dtype=torch.float32, device="cuda")
+    dpos = torch.tensor(pos, **f32)
+    dF = torch.tensor(rng.normal(size=(N, 3)), **f32)
+    dT = torch.tensor(rng.normal(size=(N, 3)), **f32)
+    s = NBody("open", "open", "single_wall", precision="float")
+    s.setParameters(wallHeight=0.0)
+    s.initialize(viscosity=1 / (6 * math.pi), hydrodynamicRadius=1.0, includeAngular=True)
+    s.setPositions(dpos)
+    s.Mdot(dF, dT)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        s.Mdot(dF, dT)
+    e1.record()
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3 / reps
+    pairs = float(N) * N
+    return {"workload": "single wall, N=262144, x,y ~ U[0,1024), z ~ U[1.5,40], forces + "
+                        "torques, includeAngular, FP32",
+            "mdot_ms": t * 1e3, "mdot_pair_interactions_per_s": pairs / t,
+            "achieved_tflops": pairs * FLOPS_PER_PAIR[("wall", True)] / t / 1e12}
+
+
 def cpu_baseline(w, pos, F, T, seconds=8.0):
     """FP64 C oracle (all host threads) on a bounded sample of the workload:
     the first R target rows against every source."""
@@ -526,6 +560,10 @@ def run_ours(args, w, ws, rank, local):
     ens = None
     if not args.skip_ensemble:
         ens = ensemble_comparison(torch, max(2, args.steps), 2, rank)
+    large = None
+    if not args.skip_large:
+        large = large_wall_mdot(torch, rank)
+        large["frac_of_fp32_peak"] = large["achieved_tflops"] / peak
 
     if rank != 0:
         return
@@ -542,6 +580,7 @@ def run_ours(args, w, ws, rank, local):
                       "preconditioner": "none (plain Lanczos)"},
         "sqrtMdotW_learned_vs_plain": cmp,
         "ensemble_256": ens,
+        "wall_262k_mdot": large,
         "mdot_pair_interactions_per_s": pairs / t_mdot,
         "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
@@ -569,6 +608,8 @@ def main():
                     help="skip the plain vs learned-preconditioner sqrtMdotW comparison")
     ap.add_argument("--skip-ensemble", action="store_true",
                     help="skip the batched ensemble of 256 uneven systems")
+    ap.add_argument("--skip-large", action="store_true",
+                    help="skip the N = 262144 single-wall Mdot")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     ws, rank, local = dist_setup()
