@@ -2,8 +2,11 @@
 // training: k-nearest neighbours, feature/MLP/rotation build of P, sparse P
 // and P^T products, and the dense GEMM / activation / loss / Adam kernels the
 // training loop is made of.
+#include <algorithm>
 #include <cfloat>
+#include <cmath>
 #include <cstdint>
+#include <cstring>
 
 #include "launch_count.hpp"
 #include "precond.cuh"
@@ -11,49 +14,142 @@
 namespace lmg {
 
 // ---------------------------------------------------------------------------
-// k nearest neighbours within each batch (self first), brute force through
-// shared-memory tiles: O(N * batch) distance tests, ~1 ms at N = 65536.
+// k nearest neighbours within each batch (self first) on a uniform grid.
+// The bounding box sets a cell side h for ~4 particles per cell on average;
+// particles are counted into cells keyed by (batch, cell), the counts are
+// scanned and the particles sorted by cell; then each particle searches the
+// cells around its own in shells of Chebyshev distance 0, 1, 2, ... and stops
+// once its K-th nearest squared distance is at most (s h)^2: every point
+// closer than s h lies in a cell at Chebyshev distance <= s, so the list is
+// exact.  Cost O(N x particles in the searched cells) instead of O(N^2).
 // ---------------------------------------------------------------------------
 constexpr int kKnnThreads = 128;
+constexpr int kScanThreads = 1024;
+
+// order-preserving map of floats to unsigned (for atomic min / max)
+__device__ __forceinline__ unsigned ord_key(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ inline float ord_float(unsigned u) {
+  u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+  float f;
+  std::memcpy(&f, &u, sizeof(f));
+  return f;
+}
+
+// box[0..2] = keys of the minima (start 0xffffffff), box[3..5] of the maxima (start 0)
+__global__ void knn_box_kernel(const float *__restrict__ pos, int N, unsigned *box) {
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      lo[c] = fminf(lo[c], pos[3 * i + c]);
+      hi[c] = fmaxf(hi[c], pos[3 * i + c]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+      hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(box + c, ord_key(lo[c]));
+      atomicMax(box + 3 + c, ord_key(hi[c]));
+    }
+  }
+}
+
+struct KnnGridShape {
+  float x0, y0, z0, inv_h, h;
+  int nx, ny, nz, cells;  // cells per batch
+  int nper;
+};
+
+__device__ __forceinline__ int cell_coord(float v, float v0, float inv_h, int n) {
+  const int c = (int)((v - v0) * inv_h);
+  return c < 0 ? 0 : (c >= n ? n - 1 : c);
+}
+
+__global__ void knn_key_kernel(const float *__restrict__ pos, int N, KnnGridShape g, int *key,
+                               int *cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int ix = cell_coord(pos[3 * i], g.x0, g.inv_h, g.nx);
+  const int iy = cell_coord(pos[3 * i + 1], g.y0, g.inv_h, g.ny);
+  const int iz = cell_coord(pos[3 * i + 2], g.z0, g.inv_h, g.nz);
+  const int k = (i / g.nper) * g.cells + (ix * g.ny + iy) * g.nz + iz;
+  key[i] = k;
+  atomicAdd(cnt + k, 1);
+}
+
+// exclusive scan of cnt[0..T) into start[0..T] (start[T] = total), one CTA
+__global__ void __launch_bounds__(kScanThreads)
+knn_scan_kernel(const int *__restrict__ cnt, int T, int *__restrict__ start) {
+  __shared__ int part[kScanThreads];
+  const int per = (T + kScanThreads - 1) / kScanThreads;
+  const int b = threadIdx.x * per, e = min(T, b + per);
+  int sum = 0;
+  for (int k = b; k < e; k++) sum += cnt[k];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < kScanThreads; o <<= 1) {  // inclusive Hillis-Steele scan
+    const int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = part[threadIdx.x] - sum;
+  for (int k = b; k < e; k++) {
+    start[k] = run;
+    run += cnt[k];
+  }
+  if (threadIdx.x == kScanThreads - 1) start[T] = part[kScanThreads - 1];
+}
+
+__global__ void knn_scatter_kernel(const float *__restrict__ pos, int N, const int *key,
+                                   const int *start, int *fill, int *sidx, float4 *spos) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int k = key[i];
+  const int slot = start[k] + atomicAdd(fill + k, 1);
+  sidx[slot] = i;
+  spos[slot] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.f);
+}
 
 template <int KB>
 __global__ void __launch_bounds__(kKnnThreads)
-knn_kernel(const float *__restrict__ pos, int N, int nper, int *__restrict__ nb) {
-  __shared__ float sx[kKnnThreads], sy[kKnnThreads], sz[kKnnThreads];
+knn_search_kernel(const float *__restrict__ pos, int N, KnnGridShape g,
+                  const int *__restrict__ start, const int *__restrict__ sidx,
+                  const float4 *__restrict__ spos, int *__restrict__ nb) {
   const int i = blockIdx.x * kKnnThreads + threadIdx.x;
-  const int ic = i < N ? i : N - 1;
-  const float xi = pos[3 * ic], yi = pos[3 * ic + 1], zi = pos[3 * ic + 2];
-  const int b0 = (ic / nper) * nper;
-  const int b1 = min(N, b0 + nper);
-  const int first = blockIdx.x * kKnnThreads;
-  const int last = min(N, first + kKnnThreads) - 1;
-  const int s0 = (first / nper) * nper;
-  const int s1 = min(N, (last / nper + 1) * nper);
+  if (i >= N) return;
+  const float xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+  const int ix = cell_coord(xi, g.x0, g.inv_h, g.nx);
+  const int iy = cell_coord(yi, g.y0, g.inv_h, g.ny);
+  const int iz = cell_coord(zi, g.z0, g.inv_h, g.nz);
+  const int base = (i / g.nper) * g.cells;
   float bd[KB];
   int bj[KB];
 #pragma unroll
   for (int q = 0; q < KB; q++) {
     bd[q] = FLT_MAX;
-    bj[q] = ic;
+    bj[q] = i;
   }
-  for (int ts = s0; ts < s1; ts += kKnnThreads) {
-    const int j = ts + threadIdx.x;
-    if (j < s1) {
-      sx[threadIdx.x] = pos[3 * j];
-      sy[threadIdx.x] = pos[3 * j + 1];
-      sz[threadIdx.x] = pos[3 * j + 2];
-    }
-    __syncthreads();
-    const int nh = min(kKnnThreads, s1 - ts);
-    for (int jj = 0; jj < nh; jj++) {
-      const int j2 = ts + jj;
-      const float dx = sx[jj] - xi, dy = sy[jj] - yi, dz = sz[jj] - zi;
+  auto scan_cell = [&](int cx, int cy, int cz) {
+    const int k = base + (cx * g.ny + cy) * g.nz + cz;
+    const int e = start[k + 1];
+    for (int t = start[k]; t < e; t++) {
+      const float4 p = spos[t];
+      const float dx = p.x - xi, dy = p.y - yi, dz = p.z - zi;
       const float d = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      if (d < bd[KB - 1] && j2 >= b0 && j2 < b1) {
+      if (d < bd[KB - 1]) {
         // insertion into the sorted list, unrolled so it stays in registers;
-        // the particle itself (d = 0) lands in slot 0
-        float cd = (j2 == ic) ? -1.0f : d;
-        int cj = j2;
+        // the particle itself lands in slot 0
+        const int j = sidx[t];
+        const float cd = (j == i) ? -1.0f : d;
         bool placed = false;
 #pragma unroll
         for (int q = KB - 1; q >= 1; q--) {
@@ -63,62 +159,137 @@ knn_kernel(const float *__restrict__ pos, int N, int nper, int *__restrict__ nb)
               bj[q] = bj[q - 1];
             } else {
               bd[q] = cd;
-              bj[q] = cj;
+              bj[q] = j;
               placed = true;
             }
           }
         }
         if (!placed) {
           bd[0] = cd;
-          bj[0] = cj;
+          bj[0] = j;
         }
       }
     }
-    __syncthreads();
+  };
+  const int smax = max(g.nx, max(g.ny, g.nz));
+  for (int s = 0; s <= smax; s++) {
+    // the cells at Chebyshev distance exactly s
+    for (int dx = -s; dx <= s; dx++) {
+      const int cx = ix + dx;
+      if (cx < 0 || cx >= g.nx) continue;
+      for (int dy = -s; dy <= s; dy++) {
+        const int cy = iy + dy;
+        if (cy < 0 || cy >= g.ny) continue;
+        const bool face = (dx == -s || dx == s || dy == -s || dy == s);
+        for (int dz = -s; dz <= s; dz += face ? 1 : (s > 0 ? 2 * s : 1)) {
+          const int cz = iz + dz;
+          if (cz >= 0 && cz < g.nz) scan_cell(cx, cy, cz);
+        }
+      }
+    }
+    const float r = s * g.h;
+    if (bd[KB - 1] <= r * r) break;
   }
-  if (i < N) {
 #pragma unroll
-    for (int q = 0; q < KB; q++) nb[(size_t)i * KB + q] = bj[q];
-  }
+  for (int q = 0; q < KB; q++) nb[(size_t)i * KB + q] = bj[q];
 }
 
-cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaStream_t stream) {
-  const int blocks = (N + kKnnThreads - 1) / kKnnThreads;
+cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaStream_t stream,
+                       KnnScratch *scratch) {
   if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
+  if (N <= 0) return cudaSuccess;
+  KnnScratch local;
+  KnnScratch &w = scratch ? *scratch : local;
+  if (nper <= 0 || nper > N) nper = N;
+  const int nbat = (N + nper - 1) / nper;
+  // bounding box (one small copy back to the host)
+  unsigned *box = w.box.ensure(6);
+  cudaError_t e = cudaMemsetAsync(box, 0xff, 3 * sizeof(unsigned), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(box + 3, 0, 3 * sizeof(unsigned), stream);
+  if (e != cudaSuccess) return e;
   count_launch();
-  if (K == 16) knn_kernel<17><<<blocks, kKnnThreads, 0, stream>>>(pos, N, nper, nb);
-  if (K == 32) knn_kernel<33><<<blocks, kKnnThreads, 0, stream>>>(pos, N, nper, nb);
-  if (K == 48) knn_kernel<49><<<blocks, kKnnThreads, 0, stream>>>(pos, N, nper, nb);
-  return cudaGetLastError();
+  knn_box_kernel<<<std::min((N + 255) / 256, 1024), 256, 0, stream>>>(pos, N, box);
+  unsigned *hb = w.hbox.ensure(6);
+  e = cudaMemcpyAsync(hb, box, 6 * sizeof(unsigned), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return e;
+  float lo[3], ext[3];
+  for (int c = 0; c < 3; c++) {
+    lo[c] = ord_float(hb[c]);
+    ext[c] = std::max(ord_float(hb[3 + c]) - lo[c], 1e-3f);
+  }
+  if (!std::isfinite(ext[0] + ext[1] + ext[2])) return cudaErrorInvalidValue;
+  // cell side for ~4 particles per cell of a batch; at most 2^24 cells in all
+  const double per_batch = (double)N / nbat;
+  double h = std::cbrt((double)ext[0] * ext[1] * ext[2] * 4.0 / per_batch);
+  const double cap = std::min(4.0 * per_batch + 64.0, (double)(1 << 24) / nbat);
+  int dims[3];
+  for (int it = 0; it < 64; it++) {
+    double cells = 1;
+    for (int c = 0; c < 3; c++) {
+      dims[c] = std::max(1, std::min(1 << 20, (int)std::ceil(ext[c] / h)));
+      cells *= dims[c];
+    }
+    if (cells <= cap) break;
+    h *= 1.25;
+  }
+  KnnGridShape g;
+  g.x0 = lo[0];
+  g.y0 = lo[1];
+  g.z0 = lo[2];
+  g.h = (float)h;
+  g.inv_h = (float)(1.0 / h);
+  g.nx = dims[0];
+  g.ny = dims[1];
+  g.nz = dims[2];
+  g.cells = dims[0] * dims[1] * dims[2];
+  g.nper = nper;
+  const int T = nbat * g.cells;
+  int *key = w.key.ensure(N);
+  int *cnt = w.cnt.ensure((size_t)T + 1);
+  int *start = w.start.ensure((size_t)T + 1);
+  int *sidx = w.sidx.ensure(N);
+  float4 *spos = w.spos.ensure(N);
+  e = cudaMemsetAsync(cnt, 0, ((size_t)T + 1) * sizeof(int), stream);
+  if (e != cudaSuccess) return e;
+  const int grid = (N + 255) / 256;
+  count_launch();
+  knn_key_kernel<<<grid, 256, 0, stream>>>(pos, N, g, key, cnt);
+  count_launch();
+  knn_scan_kernel<<<1, kScanThreads, 0, stream>>>(cnt, T, start);
+  e = cudaMemsetAsync(cnt, 0, ((size_t)T + 1) * sizeof(int), stream);  // reused as fill counts
+  if (e != cudaSuccess) return e;
+  count_launch();
+  knn_scatter_kernel<<<grid, 256, 0, stream>>>(pos, N, key, start, cnt, sidx, spos);
+  const int sg = (N + kKnnThreads - 1) / kKnnThreads;
+  count_launch();
+  if (K == 16) knn_search_kernel<17><<<sg, kKnnThreads, 0, stream>>>(pos, N, g, start, sidx, spos, nb);
+  if (K == 32) knn_search_kernel<33><<<sg, kKnnThreads, 0, stream>>>(pos, N, g, start, sidx, spos, nb);
+  if (K == 48) knn_search_kernel<49><<<sg, kKnnThreads, 0, stream>>>(pos, N, g, start, sidx, spos, nb);
+  e = cudaGetLastError();
+  if (e == cudaSuccess && !scratch) e = cudaStreamSynchronize(stream);  // before `local` goes
+  return e;
 }
 
 // ---------------------------------------------------------------------------
-// P rows: canonical frame, features, MLP, rotation back to the lab frame.
-// One thread per particle; the network parameters sit in shared memory and
-// are read by broadcast; activations stay in registers (fully unrolled).
+// P rows: canonical frame and features (one thread per particle), the MLP as
+// three GEMMs over all particles (gemm_launch below, bias and tanh fused),
+// then the blocks rotated back to the lab frame (one thread per block).
 // ---------------------------------------------------------------------------
 constexpr int kBuildThreads = 128;
 
 template <int K>
 __global__ void __launch_bounds__(kBuildThreads)
-precond_build_kernel(const float *__restrict__ pos, const int *__restrict__ nb, int N,
-                     const float *__restrict__ params, float inv_a, float scale,
-                     float *__restrict__ blocks) {
-  using S = PrecNet<K>;
-  constexpr int kPrecK = K, KB_ = S::Blocks, kPrecIn = S::In, kPrecHidden = S::Hidden,
-                kPrecOut = S::Out, kPrecParams = S::Params, kPrecW1 = S::W1, kPrecB1 = S::B1,
-                kPrecW2 = S::W2, kPrecB2 = S::B2, kPrecW3 = S::W3, kPrecB3 = S::B3,
-                kPrecXm = S::Xm, kPrecXs = S::Xs, kPrecYm = S::Ym, kPrecYs = S::Ys;
-  extern __shared__ float sw[];
-  for (int t = threadIdx.x; t < kPrecParams; t += kBuildThreads) sw[t] = params[t];
-  __syncthreads();
+precond_features_kernel(const float *__restrict__ pos, const int *__restrict__ nb, int N,
+                        const float *__restrict__ xmean, const float *__restrict__ xstd,
+                        float inv_a, float *__restrict__ X, float *__restrict__ E) {
   const int i = blockIdx.x * kBuildThreads + threadIdx.x;
   if (i >= N) return;
-  const int *nbi = nb + (size_t)i * KB_;
+  const int *nbi = nb + (size_t)i * (K + 1);
   const float xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
-  float rel[kPrecK][3];
+  float rel[K][3];
 #pragma unroll
-  for (int n = 0; n < kPrecK; n++) {
+  for (int n = 0; n < K; n++) {
     const int j = nbi[n + 1];
     rel[n][0] = (pos[3 * j] - xi) * inv_a;
     rel[n][1] = (pos[3 * j + 1] - yi) * inv_a;
@@ -136,7 +307,7 @@ precond_build_kernel(const float *__restrict__ pos, const int *__restrict__ nb, 
     float y0 = 0.f, y1 = 1.f, y2 = 0.f;
     bool found = false;
 #pragma unroll
-    for (int n = 1; n < kPrecK; n++) {
+    for (int n = 1; n < K; n++) {
       if (!found) {
         const float p = rel[n][0] * e[0][0] + rel[n][1] * e[0][1] + rel[n][2] * e[0][2];
         const float a0 = rel[n][0] - p * e[0][0], a1 = rel[n][1] - p * e[0][1],
@@ -158,94 +329,114 @@ precond_build_kernel(const float *__restrict__ pos, const int *__restrict__ nb, 
     e[2][1] = e[0][2] * y0 - e[0][0] * y2;
     e[2][2] = e[0][0] * y1 - e[0][1] * y0;
   }
-  float x[kPrecIn];
+  float *x = X + (size_t)i * 3 * K;
 #pragma unroll
-  for (int n = 0; n < kPrecK; n++) {
+  for (int n = 0; n < K; n++) {
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       const float v = rel[n][0] * e[c][0] + rel[n][1] * e[c][1] + rel[n][2] * e[c][2];
-      x[3 * n + c] = (v - sw[kPrecXm + 3 * n + c]) / sw[kPrecXs + 3 * n + c];
+      x[3 * n + c] = (v - xmean[3 * n + c]) / xstd[3 * n + c];
     }
   }
-  float h1[kPrecHidden];
 #pragma unroll
-  for (int j = 0; j < kPrecHidden; j++) {
-    float acc = sw[kPrecB1 + j];
+  for (int r = 0; r < 3; r++)
 #pragma unroll
-    for (int k = 0; k < kPrecIn; k++) acc = fmaf(x[k], sw[kPrecW1 + k * kPrecHidden + j], acc);
-    h1[j] = tanhf(acc);
-  }
-  float h2[kPrecHidden];
-#pragma unroll
-  for (int j = 0; j < kPrecHidden; j++) {
-    float acc = sw[kPrecB2 + j];
-#pragma unroll
-    for (int k = 0; k < kPrecHidden; k++)
-      acc = fmaf(h1[k], sw[kPrecW2 + k * kPrecHidden + j], acc);
-    h2[j] = tanhf(acc);
-  }
-  float *out = blocks + (size_t)i * KB_ * 9;
-  // output unit o, de-normalised
-  auto unit = [&](int o) {
-    float acc = sw[kPrecB3 + o];
-#pragma unroll
-    for (int k = 0; k < kPrecHidden; k++) acc = fmaf(h2[k], sw[kPrecW3 + k * kPrecOut + o], acc);
-    return acc * sw[kPrecYs + o] + sw[kPrecYm + o];
-  };
-#pragma unroll 1
-  for (int n = 0; n < KB_; n++) {
-    float b[3][3];
-    if (n == 0) {  // symmetric self block from 6 units: 00 01 02 11 12 22
-      const float u0 = unit(0), u1 = unit(1), u2 = unit(2), u3 = unit(3), u4 = unit(4),
-                  u5 = unit(5);
-      b[0][0] = u0; b[0][1] = u1; b[0][2] = u2;
-      b[1][0] = u1; b[1][1] = u3; b[1][2] = u4;
-      b[2][0] = u2; b[2][1] = u4; b[2][2] = u5;
-    } else {
-      const int o = 6 + 9 * (n - 1);
-#pragma unroll
-      for (int r = 0; r < 3; r++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) b[r][c] = unit(o + 3 * r + c);
-    }
-    // lab block = E^T b E  (E rows are the canonical axes)
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        float acc = 0.f;
-#pragma unroll
-        for (int p = 0; p < 3; p++) {
-          const float t = b[p][0] * e[0][c] + b[p][1] * e[1][c] + b[p][2] * e[2][c];
-          acc = fmaf(e[p][r], t, acc);
-        }
-        out[9 * n + 3 * r + c] = acc * scale;
-      }
-    }
-  }
+    for (int c = 0; c < 3; c++) E[9 * (size_t)i + 3 * r + c] = e[r][c];
 }
 
+// One thread per (particle, block n): de-normalised outputs -> block in the
+// canonical frame (n = 0: symmetric self block from 6 units 00 01 02 11 12
+// 22; n > 0: 9 units) -> lab frame E^T b E, times scale.
 template <int K>
-cudaError_t precond_build_k(const float *pos, const int *nb, int N, const float *params,
-                            float inv_a, float scale, float *blocks, cudaStream_t stream) {
-  const size_t smem = PrecNet<K>::Params * sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(precond_build_kernel<K>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  const int nblk = (N + kBuildThreads - 1) / kBuildThreads;
-  count_launch();
-  precond_build_kernel<K><<<nblk, kBuildThreads, smem, stream>>>(pos, nb, N, params, inv_a,
-                                                                 scale, blocks);
-  return cudaGetLastError();
+__global__ void precond_assemble_kernel(const float *__restrict__ Y,
+                                        const float *__restrict__ E, int N,
+                                        const float *__restrict__ ymean,
+                                        const float *__restrict__ ystd, float scale,
+                                        float *__restrict__ blocks) {
+  constexpr int Out = 6 + 9 * K;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)N * (K + 1)) return;
+  const int i = (int)(t / (K + 1)), n = (int)(t % (K + 1));
+  const float *y = Y + (size_t)i * Out;
+  auto unit = [&](int o) { return y[o] * ystd[o] + ymean[o]; };
+  float b[3][3];
+  if (n == 0) {
+    const float u0 = unit(0), u1 = unit(1), u2 = unit(2), u3 = unit(3), u4 = unit(4),
+                u5 = unit(5);
+    b[0][0] = u0; b[0][1] = u1; b[0][2] = u2;
+    b[1][0] = u1; b[1][1] = u3; b[1][2] = u4;
+    b[2][0] = u2; b[2][1] = u4; b[2][2] = u5;
+  } else {
+    const int o = 6 + 9 * (n - 1);
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) b[r][c] = unit(o + 3 * r + c);
+  }
+  float e[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) e[r][c] = E[9 * (size_t)i + 3 * r + c];
+  float *out = blocks + (size_t)t * 9;
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float acc = 0.f;
+#pragma unroll
+      for (int p = 0; p < 3; p++) {
+        const float tt = b[p][0] * e[0][c] + b[p][1] * e[1][c] + b[p][2] * e[2][c];
+        acc = fmaf(e[p][r], tt, acc);
+      }
+      out[3 * r + c] = acc * scale;
+    }
+  }
 }
 
-cudaError_t precond_build_launch(int K, const float *pos, const int *nb, int N,
+cudaError_t gemm_launch(int ta, int tb, int M, int N, int K, const float *A, int lda,
+                        const float *B, int ldb, float *C, int ldc, const float *bias, int act,
+                        float beta, cudaStream_t s);
+
+cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const int *nb, int N,
                                  const float *params, float inv_a, float scale, float *blocks,
-                                 cudaStream_t stream) {
-  if (K == 16) return precond_build_k<16>(pos, nb, N, params, inv_a, scale, blocks, stream);
-  if (K == 32) return precond_build_k<32>(pos, nb, N, params, inv_a, scale, blocks, stream);
-  if (K == 48) return precond_build_k<48>(pos, nb, N, params, inv_a, scale, blocks, stream);
-  return cudaErrorInvalidValue;
+                                 PrecWork *work, cudaStream_t stream) {
+  if (L.K != 16 && L.K != 32 && L.K != 48) return cudaErrorInvalidValue;
+  if (N <= 0) return cudaSuccess;
+  PrecWork local;
+  PrecWork &w = work ? *work : local;
+  float *X = w.X.ensure((size_t)N * L.In);
+  float *E = w.E.ensure((size_t)N * 9);
+  float *H1 = w.H1.ensure((size_t)N * L.H);
+  float *H2 = w.H2.ensure((size_t)N * L.H);
+  float *Y = w.Y.ensure((size_t)N * L.Out);
+  const int g = (N + kBuildThreads - 1) / kBuildThreads;
+  const float *xm = params + L.Xm, *xs = params + L.Xs;
+  count_launch();
+  if (L.K == 16) precond_features_kernel<16><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
+  if (L.K == 32) precond_features_kernel<32><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
+  if (L.K == 48) precond_features_kernel<48><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = gemm_launch(0, 0, N, L.H, L.In, X, L.In, params + L.W1, L.H, H1, L.H, params + L.B1, 1,
+                    0.f, stream);
+  if (e == cudaSuccess)
+    e = gemm_launch(0, 0, N, L.H, L.H, H1, L.H, params + L.W2, L.H, H2, L.H, params + L.B2, 1,
+                    0.f, stream);
+  if (e == cudaSuccess)
+    e = gemm_launch(0, 0, N, L.Out, L.H, H2, L.H, params + L.W3, L.Out, Y, L.Out,
+                    params + L.B3, 0, 0.f, stream);
+  if (e != cudaSuccess) return e;
+  const long nblk = (long)N * (L.K + 1);
+  const int ga = (int)((nblk + 255) / 256);
+  const float *ym = params + L.Ym, *ys = params + L.Ys;
+  count_launch();
+  if (L.K == 16) precond_assemble_kernel<16><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, blocks);
+  if (L.K == 32) precond_assemble_kernel<32><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, blocks);
+  if (L.K == 48) precond_assemble_kernel<48><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, blocks);
+  e = cudaGetLastError();
+  if (e == cudaSuccess && !work) e = cudaStreamSynchronize(stream);  // before `local` goes
+  return e;
 }
 
 // ---------------------------------------------------------------------------
@@ -417,6 +608,18 @@ __global__ void adam_kernel(size_t n, float *w, const float *g, float *m, float 
   }
 }
 
+cudaError_t gemm_launch(int ta, int tb, int M, int N, int K, const float *A, int lda,
+                        const float *B, int ldb, float *C, int ldc, const float *bias, int act,
+                        float beta, cudaStream_t s) {
+  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT);
+  count_launch();
+  if (!ta && !tb) gemm_kernel<false, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
+  else if (ta && !tb) gemm_kernel<true, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
+  else if (!ta && tb) gemm_kernel<false, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
+  else gemm_kernel<true, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
+  return cudaGetLastError();
+}
+
 }  // namespace lmg
 
 using namespace lmg;
@@ -428,14 +631,8 @@ extern "C" {
 int lmg_internal_gemm(int ta, int tb, int M, int N, int K, const float *A, int lda,
                       const float *B, int ldb, float *C, int ldc, const float *bias, int act,
                       float beta, void *stream) {
-  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT);
-  cudaStream_t s = (cudaStream_t)stream;
-  count_launch();
-  if (!ta && !tb) gemm_kernel<false, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
-  else if (ta && !tb) gemm_kernel<true, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
-  else if (!ta && tb) gemm_kernel<false, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
-  else gemm_kernel<true, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
-  return (int)cudaGetLastError();
+  return (int)lmg::gemm_launch(ta, tb, M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta,
+                               (cudaStream_t)stream);
 }
 
 int lmg_internal_tanh_backward(size_t n, const float *h, float *g, void *stream) {
@@ -469,14 +666,22 @@ int lmg_internal_adam(size_t n, float *w, const float *g, float *m, float *v, fl
 }
 
 int lmg_internal_knn_k(int K, const float *pos, int N, int nper, int *nb, void *stream) {
-  return (int)knn_launch(K, pos, N, nper, nb, (cudaStream_t)stream);
+  try {
+    return (int)knn_launch(K, pos, N, nper, nb, (cudaStream_t)stream, nullptr);
+  } catch (const std::exception &) {
+    return (int)cudaErrorMemoryAllocation;
+  }
 }
 
-int lmg_internal_precond_build_k(int K, const float *pos, const int *nb, int N,
-                                 const float *params, float inv_a, float scale, float *blocks,
-                                 void *stream) {
-  return (int)precond_build_launch(K, pos, nb, N, params, inv_a, scale, blocks,
-                                   (cudaStream_t)stream);
+int lmg_internal_precond_build_kh(int K, int H, const float *pos, const int *nb, int N,
+                                  const float *params, float inv_a, float scale, float *blocks,
+                                  void *stream) {
+  try {
+    return (int)precond_build_launch(prec_layout(K, H), pos, nb, N, params, inv_a, scale,
+                                     blocks, nullptr, (cudaStream_t)stream);
+  } catch (const std::exception &) {
+    return (int)cudaErrorMemoryAllocation;
+  }
 }
 
 int lmg_internal_precond_apply_k(int K, const float *blocks, const int *nb, int N,
@@ -495,7 +700,7 @@ int lmg_internal_knn(const float *pos, int N, int nper, int *nb, void *stream) {
 
 int lmg_internal_precond_build(const float *pos, const int *nb, int N, const float *params,
                                float inv_a, float scale, float *blocks, void *stream) {
-  return lmg_internal_precond_build_k(16, pos, nb, N, params, inv_a, scale, blocks, stream);
+  return lmg_internal_precond_build_kh(16, 64, pos, nb, N, params, inv_a, scale, blocks, stream);
 }
 
 int lmg_internal_precond_apply(const float *blocks, const int *nb, int N, const float *x,

@@ -25,46 +25,74 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "common.hpp"
+
 namespace lmg {
 
-// Network shape for K neighbours (K = 16, 32 or 48): parameters and
-// normalisation, FP32, in one contiguous array:
-//   W1[3K][64] b1[64] W2[64][64] b2[64] W3[64][6+9K] b3[6+9K]
+// Network shape for K neighbours (16, 32 or 48) and hidden width H (64, 128
+// or 256): parameters and normalisation, FP32, in one contiguous array:
+//   W1[3K][H] b1[H] W2[H][H] b2[H] W3[H][6+9K] b3[6+9K]
 //   xmean[3K] xstd[3K] ymean[6+9K] ystd[6+9K]
-template <int K> struct PrecNet {
-  static constexpr int Blocks = K + 1;  // blocks per row (self first)
-  static constexpr int In = 3 * K;
-  static constexpr int Hidden = 64;
-  static constexpr int Out = 6 + 9 * K;
-  static constexpr int W1 = 0;
-  static constexpr int B1 = W1 + In * Hidden;
-  static constexpr int W2 = B1 + Hidden;
-  static constexpr int B2 = W2 + Hidden * Hidden;
-  static constexpr int W3 = B2 + Hidden;
-  static constexpr int B3 = W3 + Hidden * Out;
-  static constexpr int Xm = B3 + Out;
-  static constexpr int Xs = Xm + In;
-  static constexpr int Ym = Xs + In;
-  static constexpr int Ys = Ym + Out;
-  static constexpr int Params = Ys + Out;
+// Every (K, H) pair has a different parameter count, which identifies it.
+struct PrecLayout {
+  int K = 0, H = 0, In = 0, Out = 0;
+  int W1 = 0, B1 = 0, W2 = 0, B2 = 0, W3 = 0, B3 = 0, Xm = 0, Xs = 0, Ym = 0, Ys = 0;
+  int Params = 0;
 };
 
-// The K whose network has n parameters, or 0.
-inline int prec_k_for_params(size_t n) {
-  if (n == (size_t)PrecNet<16>::Params) return 16;
-  if (n == (size_t)PrecNet<32>::Params) return 32;
-  if (n == (size_t)PrecNet<48>::Params) return 48;
-  return 0;
+inline PrecLayout prec_layout(int K, int H) {
+  PrecLayout L;
+  L.K = K;
+  L.H = H;
+  L.In = 3 * K;
+  L.Out = 6 + 9 * K;
+  L.W1 = 0;
+  L.B1 = L.W1 + L.In * H;
+  L.W2 = L.B1 + H;
+  L.B2 = L.W2 + H * H;
+  L.W3 = L.B2 + H;
+  L.B3 = L.W3 + H * L.Out;
+  L.Xm = L.B3 + L.Out;
+  L.Xs = L.Xm + L.In;
+  L.Ym = L.Xs + L.In;
+  L.Ys = L.Ym + L.Out;
+  L.Params = L.Ys + L.Out;
+  return L;
 }
 
-// Launchers (precond.cu) for K = 16, 32 or 48.  All pointers are device
-// memory; all work goes on `stream`.  nb holds K + 1 indices per particle
-// (itself first, then the K nearest in distance order), blocks K + 1 3x3
-// blocks per particle.
-cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaStream_t stream);
-cudaError_t precond_build_launch(int K, const float *pos, const int *nb, int N,
+// The layout whose parameter count is n (K = 0 if there is none).
+inline PrecLayout prec_layout_for_params(size_t n) {
+  for (int K : {16, 32, 48})
+    for (int H : {64, 128, 256}) {
+      const PrecLayout L = prec_layout(K, H);
+      if ((size_t)L.Params == n) return L;
+    }
+  return PrecLayout{};
+}
+
+// Work arrays of the grid search, kept by the caller between calls (the
+// launcher allocates them when they are too small; it reads the bounding box
+// back, so it synchronises `stream` once).
+struct KnnScratch {
+  DeviceBuffer<unsigned> box;
+  PinnedBuffer<unsigned> hbox;
+  DeviceBuffer<int> key, cnt, start, sidx;
+  DeviceBuffer<float4> spos;
+};
+cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaStream_t stream,
+                       KnnScratch *scratch);
+// Work arrays of the build: features X [N][3K], frames E [N][9], hidden
+// activations H1, H2 [N][H], network outputs Y [N][6+9K].
+struct PrecWork {
+  DeviceBuffer<float> X, E, H1, H2, Y;
+};
+// P blocks from positions and neighbour lists: features and canonical frames
+// (one thread per particle), the three layers as GEMMs of all particles at
+// once (this library's GEMM kernel, bias and tanh fused), then the blocks
+// rotated back to the lab frame and scaled.
+cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const int *nb, int N,
                                  const float *params, float inv_a, float scale, float *blocks,
-                                 cudaStream_t stream);
+                                 PrecWork *work, cudaStream_t stream);
 // out_i = sum_n B[i][n] x_{nb[i][n]}   (P x), 3 components per particle
 cudaError_t precond_apply_launch(int K, const float *blocks, const int *nb, int N,
                                  const float *x, float *out, cudaStream_t stream);

@@ -140,8 +140,11 @@ template <class R> class Solver final : public SolverBase {
   bool prec_on_ = false;
   bool prec_dirty_ = true;
   int prec_k_ = 16;  // neighbours per row of P, from the network's parameter count
+  PrecLayout prec_layout_;
+  PrecWork prec_work_;
   DeviceBuffer<float> prec_params_, prec_blocks_;
   DeviceBuffer<int> prec_nb_;
+  KnnScratch knn_scratch_;
   DeviceBuffer<R> pt_, pu_, bx_, br_, brh_, bp_, bv_, bs_, bt_;  // operator and BiCGSTAB vectors
   int num_sms_ = 0;
   bool tickets_zeroed_ = false;
@@ -683,16 +686,16 @@ void Solver<R>::set_preconditioner(const std::string &kind, const float *params,
   if (!std::is_same<R, float>::value)
     throw Error(LMG_ERR_INVALID_ARGUMENT,
                 "[libmobility_gb300] the learned preconditioner needs precision float");
-  const int k = params ? prec_k_for_params(n) : 0;
-  if (k == 0)
+  const PrecLayout L = params ? prec_layout_for_params(n) : PrecLayout{};
+  if (L.K == 0)
     throw Error(LMG_ERR_INVALID_ARGUMENT,
-                "[libmobility_gb300] preconditioner parameters must hold " +
-                    std::to_string(PrecNet<16>::Params) + ", " +
-                    std::to_string(PrecNet<32>::Params) + " or " +
-                    std::to_string(PrecNet<48>::Params) + " floats (K = 16, 32, 48)");
+                "[libmobility_gb300] preconditioner parameters: " + std::to_string(n) +
+                    " floats is not the size of a network over K = 16, 32 or 48 neighbours "
+                    "with 64, 128 or 256 hidden units");
   float *d = prec_params_.ensure(n);
   LMG_CUDA(cudaMemcpy(d, params, n * sizeof(float), cudaMemcpyHostToDevice));
-  prec_k_ = k;
+  prec_layout_ = L;
+  prec_k_ = L.K;
   prec_on_ = true;
   prec_dirty_ = true;
 }
@@ -710,10 +713,11 @@ template <class R> void Solver<R>::prec_build() {
     const int kb = prec_k_ + 1;
     int *nb = prec_nb_.ensure((size_t)N * kb);
     float *blocks = prec_blocks_.ensure((size_t)N * kb * 9);
-    LMG_CUDA(knn_launch(prec_k_, pos_.ptr, N, batch_size(), nb, stream()));
+    LMG_CUDA(knn_launch(prec_k_, pos_.ptr, N, batch_size(), nb, stream(), &knn_scratch_));
     // targets were trained with t0 = 1: M^{-1/2} scales as t0^{-1/2}
-    LMG_CUDA(precond_build_launch(prec_k_, pos_.ptr, nb, N, prec_params_.ptr, (float)(1.0 / a_),
-                                  (float)(1.0 / std::sqrt(t0_)), blocks, stream()));
+    LMG_CUDA(precond_build_launch(prec_layout_, pos_.ptr, nb, N, prec_params_.ptr, (float)(1.0 / a_),
+                                  (float)(1.0 / std::sqrt(t0_)), blocks, &prec_work_,
+                                  stream()));
     prec_dirty_ = false;
   }
 }

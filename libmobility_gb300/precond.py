@@ -26,7 +26,7 @@ from pathlib import Path
 
 import numpy as np
 
-NH = 64
+NH = 64  # default hidden width
 WEIGHTS_DIR = Path(__file__).resolve().parent / "weights"
 
 
@@ -198,25 +198,29 @@ def make_dataset(systems, per_sys=32, seed=0, workers=None, log=None, k=16):
 # ---------------------------------------------------------------------------
 # parameters
 # ---------------------------------------------------------------------------
-def layout(k):
-    """Parameter layout for k neighbours, as csrc/precond.cuh (PrecNet<K>)."""
+def layout(k, h=NH):
+    """Parameter layout for k neighbours and h hidden units, as
+    csrc/precond.cuh (PrecLayout)."""
     nin, nout = 3 * k, 6 + 9 * k
-    return [("W1", (nin, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)),
-            ("W3", (NH, nout)), ("b3", (nout,)), ("xmean", (nin,)), ("xstd", (nin,)),
+    return [("W1", (nin, h)), ("b1", (h,)), ("W2", (h, h)), ("b2", (h,)),
+            ("W3", (h, nout)), ("b3", (nout,)), ("xmean", (nin,)), ("xstd", (nin,)),
             ("ymean", (nout,)), ("ystd", (nout,))]
 
 
-def ntrain(k):
+def ntrain(k, h=NH):
     """Length of the trainable prefix (weights and biases)."""
     nin, nout = 3 * k, 6 + 9 * k
-    return nin * NH + NH + NH * NH + NH + NH * nout + nout
+    return nin * h + h + h * h + h + h * nout + nout
 
 
-def k_of_params(n):
+def shape_of_params(n):
+    """(k, h) of a flat parameter vector of length n."""
     for k in (16, 32, 48):
-        if n == sum(int(np.prod(s)) for _, s in layout(k)):
-            return k
-    raise ValueError(f"{n} is not the parameter count of a K = 16, 32 or 48 network")
+        for h in (64, 128, 256):
+            if n == sum(int(np.prod(s)) for _, s in layout(k, h)):
+                return k, h
+    raise ValueError(f"{n} is not the parameter count of a K = 16, 32 or 48 network "
+                     "with 64, 128 or 256 hidden units")
 
 
 LAYOUT = layout(16)
@@ -241,8 +245,9 @@ def load_weights(path=None):
 class GpuMLP:
     def __init__(self, lib, torch, params, stream):
         self.lib, self.torch, self.s = lib, torch, stream
-        self.k = k_of_params(len(params))
-        self.nin, self.nout, self.ntrain = 3 * self.k, 6 + 9 * self.k, ntrain(self.k)
+        self.k, self.h = shape_of_params(len(params))
+        self.nin, self.nout = 3 * self.k, 6 + 9 * self.k
+        self.ntrain = ntrain(self.k, self.h)
         self.p = torch.tensor(params, device="cuda")
         self.g = torch.zeros(self.ntrain, device="cuda")
         self.m = torch.zeros(self.ntrain, device="cuda")
@@ -251,7 +256,7 @@ class GpuMLP:
         off = 0
         self.view = {}
         self.gview = {}
-        for name, shp in layout(self.k):
+        for name, shp in layout(self.k, self.h):
             n = int(np.prod(shp))
             self.view[name] = self.p[off:off + n]
             if off < self.ntrain:
@@ -271,7 +276,7 @@ class GpuMLP:
     def forward(self, X, H1, H2, Yp):
         B = X.shape[0]
         v = self.view
-        NIN, NOUT = self.nin, self.nout
+        NIN, NOUT, NH = self.nin, self.nout, self.h
         self.gemm(0, 0, B, NH, NIN, X, NIN, v["W1"], NH, H1, NH, v["b1"], 1)
         self.gemm(0, 0, B, NH, NH, H1, NH, v["W2"], NH, H2, NH, v["b2"], 1)
         self.gemm(0, 0, B, NOUT, NH, H2, NH, v["W3"], NOUT, Yp, NOUT, v["b3"], 0)
@@ -279,7 +284,7 @@ class GpuMLP:
     def backward(self, X, H1, H2, Yp, T, dY, dH2, dH1):
         B = X.shape[0]
         v, g, lib = self.view, self.gview, self.lib
-        NIN, NOUT = self.nin, self.nout
+        NIN, NOUT, NH = self.nin, self.nout, self.h
         scale = ctypes.c_float(2.0 / (B * NOUT))
         assert lib.lmg_internal_mse_grad(ctypes.c_size_t(B * NOUT), self._ptr(Yp), self._ptr(T),
                                          self._ptr(dY), scale, self._ptr(self.loss), self.s) == 0
@@ -304,7 +309,7 @@ class GpuMLP:
                                           self.s) == 0
 
 
-def init_params(X, Y, seed=0):
+def init_params(X, Y, seed=0, NH=NH):
     rng = np.random.default_rng(seed)
     NIN, NOUT = X.shape[1], Y.shape[1]
     d = {}
@@ -319,14 +324,16 @@ def init_params(X, Y, seed=0):
     return d
 
 
-def train(X, Y, epochs=60, batch=4096, lr=2e-3, seed=0, log=print, val_frac=0.05):
+def train(X, Y, epochs=60, batch=4096, lr=2e-3, seed=0, log=print, val_frac=0.05, hidden=NH):
     import torch
     from . import _capi
     lib = _capi.load()
-    d = init_params(X, Y, seed)
+    NH = hidden
+    d = init_params(X, Y, seed, NH)
     k = X.shape[1] // 3
     NIN, NOUT = 3 * k, 6 + 9 * k
-    params = np.concatenate([np.asarray(d[name], np.float32).ravel() for name, _ in layout(k)])
+    params = np.concatenate([np.asarray(d[name], np.float32).ravel()
+                             for name, _ in layout(k, NH)])
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     net = GpuMLP(lib, torch, params, stream)
     xm, xs = d["xmean"].astype(np.float32), d["xstd"].astype(np.float32)
@@ -366,7 +373,8 @@ def train(X, Y, epochs=60, batch=4096, lr=2e-3, seed=0, log=print, val_frac=0.05
         hist.append((ep, train_mse, val))
         if ep % 5 == 0 or ep == epochs - 1:
             log(f"epoch {ep:3d} train mse {train_mse:.4f} val mse {val:.4f} ({time.time()-t0:.1f}s)")
-    out = {name: net.view[name].detach().cpu().numpy().reshape(shp) for name, shp in layout(k)}
+    out = {name: net.view[name].detach().cpu().numpy().reshape(shp)
+           for name, shp in layout(k, NH)}
     out["xmean"], out["xstd"], out["ymean"], out["ystd"] = xm, xs, ym, ys
     return out, hist
 
@@ -376,7 +384,7 @@ def evaluate(net, Xv, Yv, batch, torch):
     for b0 in range(0, Xv.shape[0], batch):
         xb = Xv[b0:b0 + batch].contiguous()
         B = xb.shape[0]
-        H1 = torch.empty(B, NH, device="cuda")
+        H1 = torch.empty(B, net.h, device="cuda")
         H2 = torch.empty_like(H1)
         Yp = torch.empty(B, net.nout, device="cuda")
         net.forward(xb, H1, H2, Yp)
@@ -389,6 +397,7 @@ def main():
     sub = ap.add_subparsers(dest="cmd")
     t = sub.add_parser("train")
     t.add_argument("--k", type=int, default=16, choices=[16, 32, 48])
+    t.add_argument("--hidden", type=int, default=NH, choices=[64, 128, 256])
     t.add_argument("--systems", type=int, default=20000)
     t.add_argument("--per-system", type=int, default=32)
     t.add_argument("--epochs", type=int, default=60)
@@ -400,13 +409,13 @@ def main():
         X, Y = make_dataset(a.systems, a.per_system, a.seed,
                             log=lambda m: print(m, flush=True), k=a.k)
         print(f"dataset {X.shape} {Y.shape} in {time.time()-t0:.1f}s", flush=True)
-        w, hist = train(X, Y, epochs=a.epochs, seed=a.seed)
+        w, hist = train(X, Y, epochs=a.epochs, seed=a.seed, hidden=a.hidden)
         out = a.out or str(weights_path(a.k))
         Path(out).parent.mkdir(parents=True, exist_ok=True)
         np.savez(out, **w, history=np.array(hist),
                  info=np.array(json.dumps({"systems": a.systems, "per_system": a.per_system,
                                            "epochs": a.epochs, "samples": int(X.shape[0]),
-                                           "k": a.k})))
+                                           "k": a.k, "hidden": a.hidden})))
         print("saved", out)
 
 

@@ -11,12 +11,12 @@ K = 16
 NH = 64
 
 
-def shapes(k=K):
-    """Parameter layout of the network for k neighbours (3k -> 64 -> 64 ->
-    6 + 9k)."""
+def shapes(k=K, h=NH):
+    """Parameter layout of the network for k neighbours and h hidden units
+    (3k -> h -> h -> 6 + 9k)."""
     nin, nout = 3 * k, 6 + 9 * k
-    return [("W1", (nin, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)),
-            ("W3", (NH, nout)), ("b3", (nout,)), ("xmean", (nin,)), ("xstd", (nin,)),
+    return [("W1", (nin, h)), ("b1", (h,)), ("W2", (h, h)), ("b2", (h,)),
+            ("W3", (h, nout)), ("b3", (nout,)), ("xmean", (nin,)), ("xstd", (nin,)),
             ("ymean", (nout,)), ("ystd", (nout,))]
 
 
@@ -24,17 +24,22 @@ SHAPES = shapes(K)
 NIN, NOUT = 3 * K, 6 + 9 * K
 
 
-def k_of(flat):
-    """Neighbour count of a flat parameter vector."""
+def kh_of(flat):
+    """(neighbours, hidden units) of a flat parameter vector."""
     for k in (16, 32, 48):
-        if len(flat) == sum(int(np.prod(s)) for _, s in shapes(k)):
-            return k
+        for h in (64, 128, 256):
+            if len(flat) == sum(int(np.prod(s)) for _, s in shapes(k, h)):
+                return k, h
     raise ValueError("not a preconditioner parameter vector")
+
+
+def k_of(flat):
+    return kh_of(flat)[0]
 
 
 def unpack(flat):
     out, o = {}, 0
-    for k, shp in shapes(k_of(flat)):
+    for k, shp in shapes(*kh_of(flat)):
         n = int(np.prod(shp))
         out[k] = np.asarray(flat[o:o + n], np.float64).reshape(shp)
         o += n

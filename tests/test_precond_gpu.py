@@ -107,19 +107,21 @@ def test_build_and_apply_match_oracle(cuda, po):
         assert np.allclose(out.cpu().numpy(), ref_y, rtol=1e-4, atol=1e-5 * np.abs(ref_y).max())
 
 
-@pytest.mark.parametrize("K", [32, 48])
-def test_wider_networks_match_oracle(cuda, po, K):
-    """kNN, P build and P / P^T products for networks over K = 32 and 48
-    neighbours, against the NumPy oracle."""
+@pytest.mark.parametrize("K,H", [(32, 64), (48, 64), (48, 256), (16, 128)])
+def test_wider_networks_match_oracle(cuda, po, K, H):
+    """kNN, P build and P / P^T products for networks over K = 16, 32 and
+    48 neighbours and 64 to 256 hidden units, against the NumPy oracle."""
     import torch
     lib = _lib()
-    rng = np.random.default_rng(K)
+    rng = np.random.default_rng(K + H)
     N = 200
     p = _clustered(rng, N).astype(np.float32)
-    d = {k: rng.normal(0, 0.3, shp) for k, shp in po.shapes(K)}
+    d = {k: rng.normal(0, 0.3, shp) for k, shp in po.shapes(K, H)}
+    d["W2"] *= np.sqrt(64 / H)
+    d["W3"] *= np.sqrt(64 / H)
     d["xstd"] = np.abs(d["xstd"]) + 1.0
     d["ystd"] = np.abs(d["ystd"]) + 0.5
-    params = np.concatenate([np.asarray(d[k], np.float32).ravel() for k, _ in po.shapes(K)])
+    params = np.concatenate([np.asarray(d[k], np.float32).ravel() for k, _ in po.shapes(K, H)])
     dp = torch.tensor(p, device="cuda")
     nb = torch.empty((N, K + 1), dtype=torch.int32, device="cuda")
     blocks = torch.empty((N, K + 1, 9), dtype=torch.float32, device="cuda")
@@ -127,7 +129,7 @@ def test_wider_networks_match_oracle(cuda, po, K):
     assert lib.lmg_internal_knn_k(K, ctypes.c_void_p(dp.data_ptr()), N, N,
                                   ctypes.c_void_p(nb.data_ptr()), None) == 0
     a, scale = 1.3, 0.7
-    assert lib.lmg_internal_precond_build_k(K, ctypes.c_void_p(dp.data_ptr()),
+    assert lib.lmg_internal_precond_build_kh(K, H, ctypes.c_void_p(dp.data_ptr()),
                                             ctypes.c_void_p(nb.data_ptr()), N,
                                             ctypes.c_void_p(dparams.data_ptr()), 1.0 / a, scale,
                                             ctypes.c_void_p(blocks.data_ptr()), None) == 0
