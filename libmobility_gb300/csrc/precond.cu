@@ -15,7 +15,7 @@ namespace lmg {
 
 // ---------------------------------------------------------------------------
 // k nearest neighbours within each batch (self first) on a uniform grid.
-// The bounding box sets a cell side h for ~4 particles per cell on average;
+// The bounding box sets a cell side h for a few particles per cell on average;
 // particles are counted into cells keyed by (batch, cell), the counts are
 // scanned and the particles sorted by cell; then each particle searches the
 // cells around its own in shells of Chebyshev distance 0, 1, 2, ... and stops
@@ -119,55 +119,56 @@ __global__ void knn_scatter_kernel(const float *__restrict__ pos, int N, const i
   spos[slot] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.f);
 }
 
+// Particles are taken in cell order (thread t -> sidx[t]), so the lanes of a
+// warp search the same cells: their loops stay in step and share cached reads.
+// Each thread's sorted list of the KB nearest lives in shared memory
+// (entry q of thread t at [q][t]: the lanes of a warp use distinct banks);
+// a candidate is placed by binary search and only the tail moves.
+constexpr int kSearchThreads = 64;
+
 template <int KB>
-__global__ void __launch_bounds__(kKnnThreads)
-knn_search_kernel(const float *__restrict__ pos, int N, KnnGridShape g,
-                  const int *__restrict__ start, const int *__restrict__ sidx,
-                  const float4 *__restrict__ spos, int *__restrict__ nb) {
-  const int i = blockIdx.x * kKnnThreads + threadIdx.x;
-  if (i >= N) return;
-  const float xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+__global__ void __launch_bounds__(kSearchThreads)
+knn_search_kernel(int N, KnnGridShape g, const int *__restrict__ start,
+                  const int *__restrict__ sidx, const float4 *__restrict__ spos,
+                  int *__restrict__ nb) {
+  __shared__ float ld[KB][kSearchThreads];
+  __shared__ int lj[KB][kSearchThreads];
+  const int tl = threadIdx.x;
+  const int t0 = blockIdx.x * kSearchThreads + tl;
+  if (t0 >= N) return;
+  const int i = sidx[t0];
+  const float4 pi = spos[t0];
+  const float xi = pi.x, yi = pi.y, zi = pi.z;
   const int ix = cell_coord(xi, g.x0, g.inv_h, g.nx);
   const int iy = cell_coord(yi, g.y0, g.inv_h, g.ny);
   const int iz = cell_coord(zi, g.z0, g.inv_h, g.nz);
   const int base = (i / g.nper) * g.cells;
-  float bd[KB];
-  int bj[KB];
-#pragma unroll
-  for (int q = 0; q < KB; q++) {
-    bd[q] = FLT_MAX;
-    bj[q] = i;
-  }
+  int len = 0;
+  float worst = FLT_MAX;  // ld[KB-1] once the list is full
   auto scan_cell = [&](int cx, int cy, int cz) {
     const int k = base + (cx * g.ny + cy) * g.nz + cz;
     const int e = start[k + 1];
     for (int t = start[k]; t < e; t++) {
       const float4 p = spos[t];
       const float dx = p.x - xi, dy = p.y - yi, dz = p.z - zi;
-      const float d = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      if (d < bd[KB - 1]) {
-        // insertion into the sorted list, unrolled so it stays in registers;
-        // the particle itself lands in slot 0
+      float cd = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      if (cd < worst) {
         const int j = sidx[t];
-        const float cd = (j == i) ? -1.0f : d;
-        bool placed = false;
-#pragma unroll
-        for (int q = KB - 1; q >= 1; q--) {
-          if (!placed) {
-            if (bd[q - 1] > cd) {
-              bd[q] = bd[q - 1];
-              bj[q] = bj[q - 1];
-            } else {
-              bd[q] = cd;
-              bj[q] = j;
-              placed = true;
-            }
-          }
+        if (j == i) cd = -1.0f;  // the particle itself goes first
+        int lo = 0, hi = len;    // first entry greater than cd
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (ld[mid][tl] > cd) hi = mid; else lo = mid + 1;
         }
-        if (!placed) {
-          bd[0] = cd;
-          bj[0] = j;
+        const int last = len < KB ? len : KB - 1;
+        for (int q = last; q > lo; q--) {
+          ld[q][tl] = ld[q - 1][tl];
+          lj[q][tl] = lj[q - 1][tl];
         }
+        ld[lo][tl] = cd;
+        lj[lo][tl] = j;
+        if (len < KB) len++;
+        if (len == KB) worst = ld[KB - 1][tl];
       }
     }
   };
@@ -188,10 +189,9 @@ knn_search_kernel(const float *__restrict__ pos, int N, KnnGridShape g,
       }
     }
     const float r = s * g.h;
-    if (bd[KB - 1] <= r * r) break;
+    if (len == KB && worst <= r * r) break;
   }
-#pragma unroll
-  for (int q = 0; q < KB; q++) nb[(size_t)i * KB + q] = bj[q];
+  for (int q = 0; q < KB; q++) nb[(size_t)q * N + i] = q < len ? lj[q][tl] : i;
 }
 
 cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaStream_t stream,
@@ -219,10 +219,14 @@ cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaSt
     ext[c] = std::max(ord_float(hb[3 + c]) - lo[c], 1e-3f);
   }
   if (!std::isfinite(ext[0] + ext[1] + ext[2])) return cudaErrorInvalidValue;
-  // cell side for ~4 particles per cell of a batch; at most 2^24 cells in all
+  // cell side half the expected distance r_K of the K-th neighbour at the
+  // mean density (then about 2 shells reach r_K and ~ (5 r_K / 2)^3 n
+  // candidates are examined); at most 2^24 cells in all
   const double per_batch = (double)N / nbat;
-  double h = std::cbrt((double)ext[0] * ext[1] * ext[2] * 4.0 / per_batch);
-  const double cap = std::min(4.0 * per_batch + 64.0, (double)(1 << 24) / nbat);
+  const double density = per_batch / ((double)ext[0] * ext[1] * ext[2]);
+  const double rK = std::cbrt(3.0 * (K + 1) / (4.0 * M_PI * density));
+  double h = 0.5 * rK;
+  const double cap = std::min(8.0 * per_batch + 64.0, (double)(1 << 24) / nbat);
   int dims[3];
   for (int it = 0; it < 64; it++) {
     double cells = 1;
@@ -261,11 +265,11 @@ cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaSt
   if (e != cudaSuccess) return e;
   count_launch();
   knn_scatter_kernel<<<grid, 256, 0, stream>>>(pos, N, key, start, cnt, sidx, spos);
-  const int sg = (N + kKnnThreads - 1) / kKnnThreads;
+  const int sg = (N + kSearchThreads - 1) / kSearchThreads;
   count_launch();
-  if (K == 16) knn_search_kernel<17><<<sg, kKnnThreads, 0, stream>>>(pos, N, g, start, sidx, spos, nb);
-  if (K == 32) knn_search_kernel<33><<<sg, kKnnThreads, 0, stream>>>(pos, N, g, start, sidx, spos, nb);
-  if (K == 48) knn_search_kernel<49><<<sg, kKnnThreads, 0, stream>>>(pos, N, g, start, sidx, spos, nb);
+  if (K == 16) knn_search_kernel<17><<<sg, kSearchThreads, 0, stream>>>(N, g, start, sidx, spos, nb);
+  if (K == 32) knn_search_kernel<33><<<sg, kSearchThreads, 0, stream>>>(N, g, start, sidx, spos, nb);
+  if (K == 48) knn_search_kernel<49><<<sg, kSearchThreads, 0, stream>>>(N, g, start, sidx, spos, nb);
   e = cudaGetLastError();
   if (e == cudaSuccess && !scratch) e = cudaStreamSynchronize(stream);  // before `local` goes
   return e;
@@ -285,12 +289,12 @@ precond_features_kernel(const float *__restrict__ pos, const int *__restrict__ n
                         float inv_a, float *__restrict__ X, float *__restrict__ E) {
   const int i = blockIdx.x * kBuildThreads + threadIdx.x;
   if (i >= N) return;
-  const int *nbi = nb + (size_t)i * (K + 1);
+  const int *nbi = nb + i;  // nb[n][i]
   const float xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
   float rel[K][3];
 #pragma unroll
   for (int n = 0; n < K; n++) {
-    const int j = nbi[n + 1];
+    const int j = nbi[(size_t)(n + 1) * N];
     rel[n][0] = (pos[3 * j] - xi) * inv_a;
     rel[n][1] = (pos[3 * j + 1] - yi) * inv_a;
     rel[n][2] = (pos[3 * j + 2] - zi) * inv_a;
@@ -356,7 +360,7 @@ __global__ void precond_assemble_kernel(const float *__restrict__ Y,
   constexpr int Out = 6 + 9 * K;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)N * (K + 1)) return;
-  const int i = (int)(t / (K + 1)), n = (int)(t % (K + 1));
+  const int n = (int)(t / N), i = (int)(t % N);  // consecutive threads: consecutive i
   const float *y = Y + (size_t)i * Out;
   auto unit = [&](int o) { return y[o] * ystd[o] + ymean[o]; };
   float b[3][3];
@@ -378,7 +382,7 @@ __global__ void precond_assemble_kernel(const float *__restrict__ Y,
   for (int r = 0; r < 3; r++)
 #pragma unroll
     for (int c = 0; c < 3; c++) e[r][c] = E[9 * (size_t)i + 3 * r + c];
-  float *out = blocks + (size_t)t * 9;
+  float *out = blocks + (size_t)n * 9 * N + i;  // blocks[n][e][i]
 #pragma unroll
   for (int r = 0; r < 3; r++) {
 #pragma unroll
@@ -389,7 +393,7 @@ __global__ void precond_assemble_kernel(const float *__restrict__ Y,
         const float tt = b[p][0] * e[0][c] + b[p][1] * e[1][c] + b[p][2] * e[2][c];
         acc = fmaf(e[p][r], tt, acc);
       }
-      out[3 * r + c] = acc * scale;
+      out[(size_t)(3 * r + c) * N] = acc * scale;
     }
   }
 }
@@ -447,16 +451,16 @@ __global__ void precond_apply_kernel(const float *__restrict__ B, const int *__r
                                      int N, const float *__restrict__ x, float *__restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  const float *b = B + (size_t)i * KB * 9;
-  const int *nbi = nb + (size_t)i * KB;
+  const size_t sN = (size_t)N;
   float o0 = 0.f, o1 = 0.f, o2 = 0.f;
-#pragma unroll
+#pragma unroll 7
   for (int n = 0; n < KB; n++) {
-    const int j = nbi[n];
+    const int j = nb[n * sN + i];
+    const float *b = B + (size_t)n * 9 * sN + i;  // b[e * N]: element e of block n
     const float v0 = x[3 * j], v1 = x[3 * j + 1], v2 = x[3 * j + 2];
-    o0 = fmaf(b[9 * n + 0], v0, fmaf(b[9 * n + 1], v1, fmaf(b[9 * n + 2], v2, o0)));
-    o1 = fmaf(b[9 * n + 3], v0, fmaf(b[9 * n + 4], v1, fmaf(b[9 * n + 5], v2, o1)));
-    o2 = fmaf(b[9 * n + 6], v0, fmaf(b[9 * n + 7], v1, fmaf(b[9 * n + 8], v2, o2)));
+    o0 = fmaf(b[0], v0, fmaf(b[sN], v1, fmaf(b[2 * sN], v2, o0)));
+    o1 = fmaf(b[3 * sN], v0, fmaf(b[4 * sN], v1, fmaf(b[5 * sN], v2, o1)));
+    o2 = fmaf(b[6 * sN], v0, fmaf(b[7 * sN], v1, fmaf(b[8 * sN], v2, o2)));
   }
   out[3 * i] = o0;
   out[3 * i + 1] = o1;
@@ -468,15 +472,15 @@ __global__ void precond_apply_t_kernel(const float *__restrict__ B, const int *_
                                        int N, const float *__restrict__ x, float *out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  const float *b = B + (size_t)i * KB * 9;
-  const int *nbi = nb + (size_t)i * KB;
+  const size_t sN = (size_t)N;
   const float v0 = x[3 * i], v1 = x[3 * i + 1], v2 = x[3 * i + 2];
-#pragma unroll
+#pragma unroll 7
   for (int n = 0; n < KB; n++) {
-    const int j = nbi[n];
-    atomicAdd(out + 3 * j, b[9 * n + 0] * v0 + b[9 * n + 3] * v1 + b[9 * n + 6] * v2);
-    atomicAdd(out + 3 * j + 1, b[9 * n + 1] * v0 + b[9 * n + 4] * v1 + b[9 * n + 7] * v2);
-    atomicAdd(out + 3 * j + 2, b[9 * n + 2] * v0 + b[9 * n + 5] * v1 + b[9 * n + 8] * v2);
+    const int j = nb[n * sN + i];
+    const float *b = B + (size_t)n * 9 * sN + i;
+    atomicAdd(out + 3 * j, b[0] * v0 + b[3 * sN] * v1 + b[6 * sN] * v2);
+    atomicAdd(out + 3 * j + 1, b[sN] * v0 + b[4 * sN] * v1 + b[7 * sN] * v2);
+    atomicAdd(out + 3 * j + 2, b[2 * sN] * v0 + b[5 * sN] * v1 + b[8 * sN] * v2);
   }
 }
 

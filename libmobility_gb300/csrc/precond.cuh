@@ -29,8 +29,8 @@
 
 namespace lmg {
 
-// Network shape for K neighbours (16, 32 or 48) and hidden width H (64, 128
-// or 256): parameters and normalisation, FP32, in one contiguous array:
+// Network shape for K neighbours (16, 32 or 48) and hidden width H (64, 128,
+// 256 or 512): parameters and normalisation, FP32, in one contiguous array:
 //   W1[3K][H] b1[H] W2[H][H] b2[H] W3[H][6+9K] b3[6+9K]
 //   xmean[3K] xstd[3K] ymean[6+9K] ystd[6+9K]
 // Every (K, H) pair has a different parameter count, which identifies it.
@@ -63,13 +63,19 @@ inline PrecLayout prec_layout(int K, int H) {
 // The layout whose parameter count is n (K = 0 if there is none).
 inline PrecLayout prec_layout_for_params(size_t n) {
   for (int K : {16, 32, 48})
-    for (int H : {64, 128, 256}) {
+    for (int H : {64, 128, 256, 512}) {
       const PrecLayout L = prec_layout(K, H);
       if ((size_t)L.Params == n) return L;
     }
   return PrecLayout{};
 }
 
+// Launchers (precond.cu) for K = 16, 32 or 48.  All pointers are device
+// memory; all work goes on `stream`.  Layouts, stored so that consecutive
+// particles are consecutive in memory: nb[n][i] (n = 0 the particle itself,
+// then its K nearest in distance order), blocks[n][e][i] (element e = 3 r + c
+// of block n of row i).
+//
 // Work arrays of the grid search, kept by the caller between calls (the
 // launcher allocates them when they are too small; it reads the bounding box
 // back, so it synchronises `stream` once).
@@ -93,10 +99,10 @@ struct PrecWork {
 cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const int *nb, int N,
                                  const float *params, float inv_a, float scale, float *blocks,
                                  PrecWork *work, cudaStream_t stream);
-// out_i = sum_n B[i][n] x_{nb[i][n]}   (P x), 3 components per particle
+// out_i = sum_n B[n][i] x_{nb[n][i]}   (P x), 3 components per particle
 cudaError_t precond_apply_launch(int K, const float *blocks, const int *nb, int N,
                                  const float *x, float *out, cudaStream_t stream);
-// out_{nb[i][n]} += B[i][n]^T x_i    (P^T x); out must be zeroed first
+// out_{nb[n][i]} += B[n][i]^T x_i    (P^T x); out must be zeroed first
 cudaError_t precond_apply_t_launch(int K, const float *blocks, const int *nb, int N,
                                    const float *x, float *out, cudaStream_t stream);
 

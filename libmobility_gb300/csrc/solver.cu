@@ -691,7 +691,7 @@ void Solver<R>::set_preconditioner(const std::string &kind, const float *params,
     throw Error(LMG_ERR_INVALID_ARGUMENT,
                 "[libmobility_gb300] preconditioner parameters: " + std::to_string(n) +
                     " floats is not the size of a network over K = 16, 32 or 48 neighbours "
-                    "with 64, 128 or 256 hidden units");
+                    "with 64, 128, 256 or 512 hidden units");
   float *d = prec_params_.ensure(n);
   LMG_CUDA(cudaMemcpy(d, params, n * sizeof(float), cudaMemcpyHostToDevice));
   prec_layout_ = L;

@@ -216,11 +216,11 @@ def ntrain(k, h=NH):
 def shape_of_params(n):
     """(k, h) of a flat parameter vector of length n."""
     for k in (16, 32, 48):
-        for h in (64, 128, 256):
+        for h in (64, 128, 256, 512):
             if n == sum(int(np.prod(s)) for _, s in layout(k, h)):
                 return k, h
     raise ValueError(f"{n} is not the parameter count of a K = 16, 32 or 48 network "
-                     "with 64, 128 or 256 hidden units")
+                     "with 64, 128, 256 or 512 hidden units")
 
 
 LAYOUT = layout(16)
@@ -397,7 +397,7 @@ def main():
     sub = ap.add_subparsers(dest="cmd")
     t = sub.add_parser("train")
     t.add_argument("--k", type=int, default=16, choices=[16, 32, 48])
-    t.add_argument("--hidden", type=int, default=NH, choices=[64, 128, 256])
+    t.add_argument("--hidden", type=int, default=NH, choices=[64, 128, 256, 512])
     t.add_argument("--systems", type=int, default=20000)
     t.add_argument("--per-system", type=int, default=32)
     t.add_argument("--epochs", type=int, default=60)

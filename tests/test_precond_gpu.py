@@ -51,12 +51,12 @@ def test_knn_matches_kdtree(cuda, po):
     rng = np.random.default_rng(0)
     for N, nper in ((300, 300), (600, 200), (4096, 4096)):
         p = rng.uniform(0, 20, (N, 3)).astype(np.float32)
-        nb = torch.empty((N, 17), dtype=torch.int32, device="cuda")
+        nb = torch.empty((17, N), dtype=torch.int32, device="cuda")  # nb[n][i]
         dp = torch.tensor(p, device="cuda")
         assert lib.lmg_internal_knn(ctypes.c_void_p(dp.data_ptr()), N, nper,
                                     ctypes.c_void_p(nb.data_ptr()), None) == 0
         torch.cuda.synchronize()
-        got = nb.cpu().numpy()
+        got = nb.cpu().numpy().T
         for b0 in range(0, N, nper):
             ref, _ = po.neighbours(p[b0:b0 + nper].astype(np.float64))
             ref = ref + b0
@@ -73,8 +73,8 @@ def test_build_and_apply_match_oracle(cuda, po):
     p = _clustered(rng, N).astype(np.float32)
     params = _random_params(po, rng)
     dp = torch.tensor(p, device="cuda")
-    nb = torch.empty((N, 17), dtype=torch.int32, device="cuda")
-    blocks = torch.empty((N, 17, 9), dtype=torch.float32, device="cuda")
+    nb = torch.empty((17, N), dtype=torch.int32, device="cuda")          # nb[n][i]
+    blocks = torch.empty((17, 9, N), dtype=torch.float32, device="cuda")  # blocks[n][e][i]
     dparams = torch.tensor(params, device="cuda")
     assert lib.lmg_internal_knn(ctypes.c_void_p(dp.data_ptr()), N, N,
                                 ctypes.c_void_p(nb.data_ptr()), None) == 0
@@ -86,8 +86,8 @@ def test_build_and_apply_match_oracle(cuda, po):
                                           None) == 0
     torch.cuda.synchronize()
     ref, nb_ref = po.p_blocks(p.astype(np.float64), params, a=a, scale=scale)
-    got = blocks.cpu().numpy().reshape(N, 17, 3, 3)
-    nbg = nb.cpu().numpy()
+    got = blocks.cpu().numpy().transpose(2, 0, 1).reshape(N, 17, 3, 3)
+    nbg = nb.cpu().numpy().T
     # compare row by row, matching neighbours by index
     for i in range(N):
         m = {int(j): got[i, n] for n, j in enumerate(nbg[i])}
@@ -123,8 +123,8 @@ def test_wider_networks_match_oracle(cuda, po, K, H):
     d["ystd"] = np.abs(d["ystd"]) + 0.5
     params = np.concatenate([np.asarray(d[k], np.float32).ravel() for k, _ in po.shapes(K, H)])
     dp = torch.tensor(p, device="cuda")
-    nb = torch.empty((N, K + 1), dtype=torch.int32, device="cuda")
-    blocks = torch.empty((N, K + 1, 9), dtype=torch.float32, device="cuda")
+    nb = torch.empty((K + 1, N), dtype=torch.int32, device="cuda")
+    blocks = torch.empty((K + 1, 9, N), dtype=torch.float32, device="cuda")
     dparams = torch.tensor(params, device="cuda")
     assert lib.lmg_internal_knn_k(K, ctypes.c_void_p(dp.data_ptr()), N, N,
                                   ctypes.c_void_p(nb.data_ptr()), None) == 0
@@ -135,8 +135,8 @@ def test_wider_networks_match_oracle(cuda, po, K, H):
                                             ctypes.c_void_p(blocks.data_ptr()), None) == 0
     torch.cuda.synchronize()
     ref, nb_ref = po.p_blocks(p.astype(np.float64), params, a=a, scale=scale)
-    got = blocks.cpu().numpy().reshape(N, K + 1, 3, 3)
-    nbg = nb.cpu().numpy()
+    got = blocks.cpu().numpy().transpose(2, 0, 1).reshape(N, K + 1, 3, 3)
+    nbg = nb.cpu().numpy().T
     for i in range(N):
         assert set(nbg[i]) == set(nb_ref[i])
         m = {int(j): got[i, n] for n, j in enumerate(nbg[i])}
