@@ -612,9 +612,87 @@ __global__ void adam_kernel(size_t n, float *w, const float *g, float *m, float 
   }
 }
 
+// Register-blocked form for large products: 128 x 128 tile per CTA, 16-deep
+// slabs of A and B in shared memory, 8 x 8 outputs per thread in two 4-wide
+// groups per dimension (rows 4 ty + r and 64 + 4 ty + r, columns likewise
+// with tx), so the inner loop reads shared memory as float4 without bank
+// conflicts and does 64 FMAs per 4 vector loads.  Tile loads put consecutive
+// threads on consecutive addresses for every transposition.
+constexpr int kGT2 = 128, kGK2 = 16;
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256)
+gemm_kernel2(int M, int N, int K, const float *__restrict__ A, int lda,
+             const float *__restrict__ B, int ldb, float *__restrict__ C, int ldc,
+             const float *__restrict__ bias, int act, float beta) {
+  __shared__ __align__(16) float sa[kGK2][kGT2 + 4];
+  __shared__ __align__(16) float sb[kGK2][kGT2 + 4];
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const int row0 = blockIdx.y * kGT2, col0 = blockIdx.x * kGT2;
+  float acc[8][8] = {};
+  for (int k0 = 0; k0 < K; k0 += kGK2) {
+#pragma unroll
+    for (int q = 0; q < (kGK2 * kGT2) / 256; q++) {
+      const int t = tid + 256 * q;
+      // A tile: element (mm, kk) = op(A)[row0 + mm][k0 + kk]
+      const int amm = TA ? t % kGT2 : t / kGK2, akk = TA ? t / kGT2 : t % kGK2;
+      const int gi = row0 + amm, gk = k0 + akk;
+      float va = 0.f;
+      if (gi < M && gk < K) va = TA ? A[(size_t)gk * lda + gi] : A[(size_t)gi * lda + gk];
+      sa[akk][amm] = va;
+      // B tile: element (kk, nn) = op(B)[k0 + kk][col0 + nn]
+      const int bnn = TB ? t / kGK2 : t % kGT2, bkk = TB ? t % kGK2 : t / kGT2;
+      const int gj = col0 + bnn, gk2 = k0 + bkk;
+      float vb = 0.f;
+      if (gj < N && gk2 < K) vb = TB ? B[(size_t)gj * ldb + gk2] : B[(size_t)gk2 * ldb + gj];
+      sb[bkk][bnn] = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kGK2; kk++) {
+      const float4 a0 = *reinterpret_cast<const float4 *>(&sa[kk][4 * ty]);
+      const float4 a1 = *reinterpret_cast<const float4 *>(&sa[kk][64 + 4 * ty]);
+      const float4 b0 = *reinterpret_cast<const float4 *>(&sb[kk][4 * tx]);
+      const float4 b1 = *reinterpret_cast<const float4 *>(&sb[kk][64 + 4 * tx]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int r = 0; r < 8; r++)
+#pragma unroll
+        for (int c = 0; c < 8; c++) acc[r][c] = fmaf(a[r], b[c], acc[r][c]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const int gi = row0 + (r < 4 ? 4 * ty + r : 64 + 4 * ty + r - 4);
+    if (gi >= M) continue;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const int gj = col0 + (c < 4 ? 4 * tx + c : 64 + 4 * tx + c - 4);
+      if (gj >= N) continue;
+      float v = acc[r][c];
+      if (bias) v += bias[gj];
+      if (beta != 0.f) v += beta * C[(size_t)gi * ldc + gj];
+      if (act == 1) v = tanhf(v);
+      C[(size_t)gi * ldc + gj] = v;
+    }
+  }
+}
+
 cudaError_t gemm_launch(int ta, int tb, int M, int N, int K, const float *A, int lda,
                         const float *B, int ldb, float *C, int ldc, const float *bias, int act,
                         float beta, cudaStream_t s) {
+  if ((long)M * N >= 64L * 128 * 128) {  // enough output tiles for the large form
+    dim3 grid2((N + kGT2 - 1) / kGT2, (M + kGT2 - 1) / kGT2);
+    count_launch();
+    if (!ta && !tb) gemm_kernel2<false, false><<<grid2, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
+    else if (ta && !tb) gemm_kernel2<true, false><<<grid2, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
+    else if (!ta && tb) gemm_kernel2<false, true><<<grid2, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
+    else gemm_kernel2<true, true><<<grid2, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);
+    return cudaGetLastError();
+  }
   dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT);
   count_launch();
   if (!ta && !tb) gemm_kernel<false, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta);

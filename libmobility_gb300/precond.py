@@ -30,15 +30,16 @@ NH = 64  # default hidden width
 WEIGHTS_DIR = Path(__file__).resolve().parent / "weights"
 
 
-def weights_path(k):
-    return WEIGHTS_DIR / f"precond_open_k{k}.npz"
+def weights_path(k, h=NH):
+    return WEIGHTS_DIR / (f"precond_open_k{k}.npz" if h == NH else f"precond_open_k{k}_h{h}.npz")
 
 
 def _default_weights():
-    """The shipped network with the most neighbours."""
-    for k in (48, 32, 16):
-        if weights_path(k).exists():
-            return weights_path(k)
+    """The shipped network used by setPreconditioner("mlp"): the widest one
+    present (48 neighbours, 512 hidden units, when shipped), else K = 16."""
+    for k, h in ((48, 512), (32, 256), (16, NH)):
+        if weights_path(k, h).exists():
+            return weights_path(k, h)
     return weights_path(16)
 
 
@@ -410,7 +411,7 @@ def main():
                             log=lambda m: print(m, flush=True), k=a.k)
         print(f"dataset {X.shape} {Y.shape} in {time.time()-t0:.1f}s", flush=True)
         w, hist = train(X, Y, epochs=a.epochs, seed=a.seed, hidden=a.hidden)
-        out = a.out or str(weights_path(a.k))
+        out = a.out or str(weights_path(a.k, a.hidden))
         Path(out).parent.mkdir(parents=True, exist_ok=True)
         np.savez(out, **w, history=np.array(hist),
                  info=np.array(json.dumps({"systems": a.systems, "per_system": a.per_system,

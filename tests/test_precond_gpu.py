@@ -155,6 +155,37 @@ def test_wider_networks_match_oracle(cuda, po, K, H):
         assert np.allclose(out.cpu().numpy(), ref_y, rtol=1e-4, atol=1e-5 * np.abs(ref_y).max())
 
 
+@pytest.mark.parametrize("ta,tb", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_large_gemm_matches_numpy(cuda, ta, tb):
+    """The register-blocked GEMM (used from 64 output tiles of 128 x 128 on):
+    all transpositions, ragged sizes, bias, tanh and beta, against FP64."""
+    import torch
+    lib = _lib()
+    rng = np.random.default_rng(10 * ta + tb)
+    M, N, K = 1037, 1131, 150
+    Am = rng.normal(size=(K, M) if ta else (M, K)).astype(np.float32)
+    Bm = rng.normal(size=(N, K) if tb else (K, N)).astype(np.float32)
+    bias = rng.normal(size=N).astype(np.float32)
+    C0 = rng.normal(size=(M, N)).astype(np.float32)
+    dA, dB = torch.tensor(Am, device="cuda"), torch.tensor(Bm, device="cuda")
+    dbias, dC = torch.tensor(bias, device="cuda"), torch.tensor(C0, device="cuda")
+    opA = Am.T if ta else Am
+    opB = Bm.T if tb else Bm
+    for act, beta in ((0, 0.0), (1, 0.0), (0, 0.5)):
+        dC.copy_(torch.tensor(C0))
+        rc = lib.lmg_internal_gemm(ta, tb, M, N, K, ctypes.c_void_p(dA.data_ptr()),
+                                   Am.shape[1], ctypes.c_void_p(dB.data_ptr()), Bm.shape[1],
+                                   ctypes.c_void_p(dC.data_ptr()), N,
+                                   ctypes.c_void_p(dbias.data_ptr()), act, ctypes.c_float(beta),
+                                   None)
+        assert rc == 0
+        torch.cuda.synchronize()
+        ref = opA.astype(np.float64) @ opB.astype(np.float64) + bias + beta * C0
+        if act:
+            ref = np.tanh(ref)
+        assert np.abs(dC.cpu().numpy() - ref).max() <= 1e-4 * max(1.0, np.abs(ref).max())
+
+
 def test_training_kernels_gradient_check(cuda, po):
     """Forward pass and gradients of the project's GEMM/tanh/MSE/colsum
     kernels against the NumPy oracle."""
@@ -247,12 +278,16 @@ def test_trained_network_reduces_iterations(cuda, oracle):
 
 @pytest.mark.parametrize("ang", [False, True])
 def test_trained_network_keeps_statistics(cuda, ang):
-    """Fluctuation-dissipation with the preconditioner on (N = 20, clustered),
-    KS test per component of M^{-1/2} y as in the reference tests."""
-    _trained()
+    """Fluctuation-dissipation with the preconditioner on (N = 64, clustered:
+    above the K + 1 particles the shipped network needs), KS test per
+    component of M^{-1/2} y as in the reference tests."""
+    from libmobility_gb300 import precond
+    w = precond.load_weights(_trained())
+    k, _ = precond.shape_of_params(len(w))
     from libmobility_gb300 import NBody
     rng = np.random.default_rng(6)
-    N = 20
+    N = 64
+    assert N >= k + 1
     p = _clustered(rng, N, phi=0.15, sigma=2.0)
     s = NBody("open", "open", "open", precision="float")
     s.setParameters()
