@@ -446,30 +446,50 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
 // ---------------------------------------------------------------------------
 // Sparse products with P (rows of K+1 3x3 blocks)
 // ---------------------------------------------------------------------------
-template <int KB>
-__global__ void precond_apply_kernel(const float *__restrict__ B, const int *__restrict__ nb,
-                                     int N, const float *__restrict__ x, float *__restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  const size_t sN = (size_t)N;
-  float o0 = 0.f, o1 = 0.f, o2 = 0.f;
-#pragma unroll 7
-  for (int n = 0; n < KB; n++) {
-    const int j = nb[n * sN + i];
-    const float *b = B + (size_t)n * 9 * sN + i;  // b[e * N]: element e of block n
-    const float v0 = x[3 * j], v1 = x[3 * j + 1], v2 = x[3 * j + 2];
-    o0 = fmaf(b[0], v0, fmaf(b[sN], v1, fmaf(b[2 * sN], v2, o0)));
-    o1 = fmaf(b[3 * sN], v0, fmaf(b[4 * sN], v1, fmaf(b[5 * sN], v2, o1)));
-    o2 = fmaf(b[6 * sN], v0, fmaf(b[7 * sN], v1, fmaf(b[8 * sN], v2, o2)));
-  }
-  out[3 * i] = o0;
-  out[3 * i + 1] = o1;
-  out[3 * i + 2] = o2;
-}
+// Each row is shared by kRowSplit threads (threadIdx.y), each taking every
+// kRowSplit-th block, so there are enough threads in flight to cover the
+// memory latency; threadIdx.x runs along the rows, so every load of blocks
+// and neighbour lists is coalesced.
+constexpr int kRowX = 64, kRowSplit = 4;
 
 template <int KB>
-__global__ void precond_apply_t_kernel(const float *__restrict__ B, const int *__restrict__ nb,
-                                       int N, const float *__restrict__ x, float *out) {
+__global__ void __launch_bounds__(kRowX * kRowSplit)
+precond_apply_kernel(const float *__restrict__ B, const int *__restrict__ nb, int N,
+                     const float *__restrict__ x, float *__restrict__ out) {
+  __shared__ float part[kRowSplit][3][kRowX];
+  const int i = blockIdx.x * kRowX + threadIdx.x;
+  const int q = threadIdx.y;
+  const size_t sN = (size_t)N;
+  float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+  if (i < N) {
+#pragma unroll 4
+    for (int n = q; n < KB; n += kRowSplit) {
+      const int j = nb[n * sN + i];
+      const float *b = B + (size_t)n * 9 * sN + i;  // b[e * N]: element e of block n
+      const float v0 = x[3 * j], v1 = x[3 * j + 1], v2 = x[3 * j + 2];
+      o0 = fmaf(b[0], v0, fmaf(b[sN], v1, fmaf(b[2 * sN], v2, o0)));
+      o1 = fmaf(b[3 * sN], v0, fmaf(b[4 * sN], v1, fmaf(b[5 * sN], v2, o1)));
+      o2 = fmaf(b[6 * sN], v0, fmaf(b[7 * sN], v1, fmaf(b[8 * sN], v2, o2)));
+    }
+  }
+  part[q][0][threadIdx.x] = o0;
+  part[q][1][threadIdx.x] = o1;
+  part[q][2][threadIdx.x] = o2;
+  __syncthreads();
+  if (q < 3 && i < N) {  // thread row q writes component q, summing the groups in order
+    float t = 0.f;
+#pragma unroll
+    for (int g = 0; g < kRowSplit; g++) t += part[g][q][threadIdx.x];
+    out[3 * i + q] = t;
+  }
+}
+
+// P^T x: one thread per row scatters with atomics (splitting the row over
+// more threads, as in the product above, made the atomics slower)
+template <int KB>
+__global__ void __launch_bounds__(256)
+precond_apply_t_kernel(const float *__restrict__ B, const int *__restrict__ nb, int N,
+                       const float *__restrict__ x, float *out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const size_t sN = (size_t)N;
@@ -486,23 +506,23 @@ __global__ void precond_apply_t_kernel(const float *__restrict__ B, const int *_
 
 cudaError_t precond_apply_launch(int K, const float *blocks, const int *nb, int N,
                                  const float *x, float *out, cudaStream_t stream) {
-  const int g = (N + 255) / 256;
+  const dim3 g((N + kRowX - 1) / kRowX), blk(kRowX, kRowSplit);
   if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
   count_launch();
-  if (K == 16) precond_apply_kernel<17><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
-  if (K == 32) precond_apply_kernel<33><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
-  if (K == 48) precond_apply_kernel<49><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 16) precond_apply_kernel<17><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 32) precond_apply_kernel<33><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 48) precond_apply_kernel<49><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
   return cudaGetLastError();
 }
 
 cudaError_t precond_apply_t_launch(int K, const float *blocks, const int *nb, int N,
                                    const float *x, float *out, cudaStream_t stream) {
-  const int g = (N + 255) / 256;
+  const dim3 g((N + 255) / 256), blk(256);
   if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
   count_launch();
-  if (K == 16) precond_apply_t_kernel<17><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
-  if (K == 32) precond_apply_t_kernel<33><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
-  if (K == 48) precond_apply_t_kernel<49><<<g, 256, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 16) precond_apply_t_kernel<17><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 32) precond_apply_t_kernel<33><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 48) precond_apply_t_kernel<49><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
   return cudaGetLastError();
 }
 
