@@ -8,10 +8,19 @@
 #include <cstdint>
 #include <cstring>
 
+#include <cuda_fp16.h>
+
 #include "launch_count.hpp"
 #include "precond.cuh"
 
 namespace lmg {
+
+// P blocks are stored as float or as half (unit scale; products apply the
+// scale): loads and stores through these two overloads
+__device__ __forceinline__ float ldf(const float *p) { return *p; }
+__device__ __forceinline__ float ldf(const __half *p) { return __half2float(*p); }
+__device__ __forceinline__ void stf(float *p, float v) { *p = v; }
+__device__ __forceinline__ void stf(__half *p, float v) { *p = __float2half_rn(v); }
 
 // ---------------------------------------------------------------------------
 // k nearest neighbours within each batch (self first) on a uniform grid.
@@ -351,12 +360,12 @@ precond_features_kernel(const float *__restrict__ pos, const int *__restrict__ n
 // One thread per (particle, block n): de-normalised outputs -> block in the
 // canonical frame (n = 0: symmetric self block from 6 units 00 01 02 11 12
 // 22; n > 0: 9 units) -> lab frame E^T b E, times scale.
-template <int K>
+template <int K, class T>
 __global__ void precond_assemble_kernel(const float *__restrict__ Y,
                                         const float *__restrict__ E, int N,
                                         const float *__restrict__ ymean,
                                         const float *__restrict__ ystd, float scale,
-                                        float *__restrict__ blocks) {
+                                        T *__restrict__ blocks) {
   constexpr int Out = 6 + 9 * K;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)N * (K + 1)) return;
@@ -382,7 +391,7 @@ __global__ void precond_assemble_kernel(const float *__restrict__ Y,
   for (int r = 0; r < 3; r++)
 #pragma unroll
     for (int c = 0; c < 3; c++) e[r][c] = E[9 * (size_t)i + 3 * r + c];
-  float *out = blocks + (size_t)n * 9 * N + i;  // blocks[n][e][i]
+  T *out = blocks + (size_t)n * 9 * N + i;  // blocks[n][e][i]
 #pragma unroll
   for (int r = 0; r < 3; r++) {
 #pragma unroll
@@ -393,7 +402,7 @@ __global__ void precond_assemble_kernel(const float *__restrict__ Y,
         const float tt = b[p][0] * e[0][c] + b[p][1] * e[1][c] + b[p][2] * e[2][c];
         acc = fmaf(e[p][r], tt, acc);
       }
-      out[(size_t)(3 * r + c) * N] = acc * scale;
+      stf(out + (size_t)(3 * r + c) * N, acc * scale);
     }
   }
 }
@@ -403,8 +412,8 @@ cudaError_t gemm_launch(int ta, int tb, int M, int N, int K, const float *A, int
                         float beta, cudaStream_t s);
 
 cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const int *nb, int N,
-                                 const float *params, float inv_a, float scale, float *blocks,
-                                 PrecWork *work, cudaStream_t stream) {
+                                 const float *params, float inv_a, float scale, void *blocks,
+                                 bool half, PrecWork *work, cudaStream_t stream) {
   if (L.K != 16 && L.K != 32 && L.K != 48) return cudaErrorInvalidValue;
   if (N <= 0) return cudaSuccess;
   PrecWork local;
@@ -435,9 +444,14 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
   const int ga = (int)((nblk + 255) / 256);
   const float *ym = params + L.Ym, *ys = params + L.Ys;
   count_launch();
-  if (L.K == 16) precond_assemble_kernel<16><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, blocks);
-  if (L.K == 32) precond_assemble_kernel<32><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, blocks);
-  if (L.K == 48) precond_assemble_kernel<48><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, blocks);
+  float *bf = static_cast<float *>(blocks);
+  __half *bh = static_cast<__half *>(blocks);
+  if (L.K == 16 && half) precond_assemble_kernel<16><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bh);
+  if (L.K == 32 && half) precond_assemble_kernel<32><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bh);
+  if (L.K == 48 && half) precond_assemble_kernel<48><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bh);
+  if (L.K == 16 && !half) precond_assemble_kernel<16><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bf);
+  if (L.K == 32 && !half) precond_assemble_kernel<32><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bf);
+  if (L.K == 48 && !half) precond_assemble_kernel<48><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bf);
   e = cudaGetLastError();
   if (e == cudaSuccess && !work) e = cudaStreamSynchronize(stream);  // before `local` goes
   return e;
@@ -452,10 +466,10 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
 // and neighbour lists is coalesced.
 constexpr int kRowX = 64, kRowSplit = 4;
 
-template <int KB>
+template <int KB, class T>
 __global__ void __launch_bounds__(kRowX * kRowSplit)
-precond_apply_kernel(const float *__restrict__ B, const int *__restrict__ nb, int N,
-                     const float *__restrict__ x, float *__restrict__ out) {
+precond_apply_kernel(const T *__restrict__ B, const int *__restrict__ nb, int N,
+                     const float *__restrict__ x, float *__restrict__ out, float scale) {
   __shared__ float part[kRowSplit][3][kRowX];
   const int i = blockIdx.x * kRowX + threadIdx.x;
   const int q = threadIdx.y;
@@ -465,11 +479,11 @@ precond_apply_kernel(const float *__restrict__ B, const int *__restrict__ nb, in
 #pragma unroll 4
     for (int n = q; n < KB; n += kRowSplit) {
       const int j = nb[n * sN + i];
-      const float *b = B + (size_t)n * 9 * sN + i;  // b[e * N]: element e of block n
+      const T *b = B + (size_t)n * 9 * sN + i;  // b[e * N]: element e of block n
       const float v0 = x[3 * j], v1 = x[3 * j + 1], v2 = x[3 * j + 2];
-      o0 = fmaf(b[0], v0, fmaf(b[sN], v1, fmaf(b[2 * sN], v2, o0)));
-      o1 = fmaf(b[3 * sN], v0, fmaf(b[4 * sN], v1, fmaf(b[5 * sN], v2, o1)));
-      o2 = fmaf(b[6 * sN], v0, fmaf(b[7 * sN], v1, fmaf(b[8 * sN], v2, o2)));
+      o0 = fmaf(ldf(b), v0, fmaf(ldf(b + sN), v1, fmaf(ldf(b + 2 * sN), v2, o0)));
+      o1 = fmaf(ldf(b + 3 * sN), v0, fmaf(ldf(b + 4 * sN), v1, fmaf(ldf(b + 5 * sN), v2, o1)));
+      o2 = fmaf(ldf(b + 6 * sN), v0, fmaf(ldf(b + 7 * sN), v1, fmaf(ldf(b + 8 * sN), v2, o2)));
     }
   }
   part[q][0][threadIdx.x] = o0;
@@ -480,50 +494,65 @@ precond_apply_kernel(const float *__restrict__ B, const int *__restrict__ nb, in
     float t = 0.f;
 #pragma unroll
     for (int g = 0; g < kRowSplit; g++) t += part[g][q][threadIdx.x];
-    out[3 * i + q] = t;
+    out[3 * i + q] = t * scale;
   }
 }
 
 // P^T x: one thread per row scatters with atomics (splitting the row over
 // more threads, as in the product above, made the atomics slower)
-template <int KB>
+template <int KB, class T>
 __global__ void __launch_bounds__(256)
-precond_apply_t_kernel(const float *__restrict__ B, const int *__restrict__ nb, int N,
-                       const float *__restrict__ x, float *out) {
+precond_apply_t_kernel(const T *__restrict__ B, const int *__restrict__ nb, int N,
+                       const float *__restrict__ x, float *out, float scale) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const size_t sN = (size_t)N;
-  const float v0 = x[3 * i], v1 = x[3 * i + 1], v2 = x[3 * i + 2];
+  const float v0 = scale * x[3 * i], v1 = scale * x[3 * i + 1], v2 = scale * x[3 * i + 2];
 #pragma unroll 7
   for (int n = 0; n < KB; n++) {
     const int j = nb[n * sN + i];
-    const float *b = B + (size_t)n * 9 * sN + i;
-    atomicAdd(out + 3 * j, b[0] * v0 + b[3 * sN] * v1 + b[6 * sN] * v2);
-    atomicAdd(out + 3 * j + 1, b[sN] * v0 + b[4 * sN] * v1 + b[7 * sN] * v2);
-    atomicAdd(out + 3 * j + 2, b[2 * sN] * v0 + b[5 * sN] * v1 + b[8 * sN] * v2);
+    const T *b = B + (size_t)n * 9 * sN + i;
+    atomicAdd(out + 3 * j, ldf(b) * v0 + ldf(b + 3 * sN) * v1 + ldf(b + 6 * sN) * v2);
+    atomicAdd(out + 3 * j + 1, ldf(b + sN) * v0 + ldf(b + 4 * sN) * v1 + ldf(b + 7 * sN) * v2);
+    atomicAdd(out + 3 * j + 2,
+              ldf(b + 2 * sN) * v0 + ldf(b + 5 * sN) * v1 + ldf(b + 8 * sN) * v2);
   }
 }
 
-cudaError_t precond_apply_launch(int K, const float *blocks, const int *nb, int N,
-                                 const float *x, float *out, cudaStream_t stream) {
-  const dim3 g((N + kRowX - 1) / kRowX), blk(kRowX, kRowSplit);
+template <int KB, class T>
+void apply_dispatch(bool transpose, const T *B, const int *nb, int N, const float *x, float *out,
+                    float scale, cudaStream_t stream) {
+  if (transpose)
+    precond_apply_t_kernel<KB, T><<<(N + 255) / 256, 256, 0, stream>>>(B, nb, N, x, out, scale);
+  else
+    precond_apply_kernel<KB, T><<<(N + kRowX - 1) / kRowX, dim3(kRowX, kRowSplit), 0, stream>>>(
+        B, nb, N, x, out, scale);
+}
+
+template <class T>
+cudaError_t apply_k(int K, bool transpose, const void *blocks, const int *nb, int N,
+                    const float *x, float *out, float scale, cudaStream_t stream) {
+  const T *B = static_cast<const T *>(blocks);
   if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
   count_launch();
-  if (K == 16) precond_apply_kernel<17><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
-  if (K == 32) precond_apply_kernel<33><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
-  if (K == 48) precond_apply_kernel<49><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
+  if (K == 16) apply_dispatch<17, T>(transpose, B, nb, N, x, out, scale, stream);
+  if (K == 32) apply_dispatch<33, T>(transpose, B, nb, N, x, out, scale, stream);
+  if (K == 48) apply_dispatch<49, T>(transpose, B, nb, N, x, out, scale, stream);
   return cudaGetLastError();
 }
 
-cudaError_t precond_apply_t_launch(int K, const float *blocks, const int *nb, int N,
-                                   const float *x, float *out, cudaStream_t stream) {
-  const dim3 g((N + 255) / 256), blk(256);
-  if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
-  count_launch();
-  if (K == 16) precond_apply_t_kernel<17><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
-  if (K == 32) precond_apply_t_kernel<33><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
-  if (K == 48) precond_apply_t_kernel<49><<<g, blk, 0, stream>>>(blocks, nb, N, x, out);
-  return cudaGetLastError();
+cudaError_t precond_apply_launch(int K, const void *blocks, bool half, float scale,
+                                 const int *nb, int N, const float *x, float *out,
+                                 cudaStream_t stream) {
+  return half ? apply_k<__half>(K, false, blocks, nb, N, x, out, scale, stream)
+              : apply_k<float>(K, false, blocks, nb, N, x, out, scale, stream);
+}
+
+cudaError_t precond_apply_t_launch(int K, const void *blocks, bool half, float scale,
+                                   const int *nb, int N, const float *x, float *out,
+                                   cudaStream_t stream) {
+  return half ? apply_k<__half>(K, true, blocks, nb, N, x, out, scale, stream)
+              : apply_k<float>(K, true, blocks, nb, N, x, out, scale, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -780,7 +809,7 @@ int lmg_internal_precond_build_kh(int K, int H, const float *pos, const int *nb,
                                   void *stream) {
   try {
     return (int)precond_build_launch(prec_layout(K, H), pos, nb, N, params, inv_a, scale,
-                                     blocks, nullptr, (cudaStream_t)stream);
+                                     blocks, false, nullptr, (cudaStream_t)stream);
   } catch (const std::exception &) {
     return (int)cudaErrorMemoryAllocation;
   }
@@ -790,9 +819,10 @@ int lmg_internal_precond_apply_k(int K, const float *blocks, const int *nb, int 
                                  const float *x, float *out, int transpose, void *stream) {
   if (transpose) {
     cudaMemsetAsync(out, 0, 3 * (size_t)N * sizeof(float), (cudaStream_t)stream);
-    return (int)precond_apply_t_launch(K, blocks, nb, N, x, out, (cudaStream_t)stream);
+    return (int)precond_apply_t_launch(K, blocks, false, 1.0f, nb, N, x, out,
+                                       (cudaStream_t)stream);
   }
-  return (int)precond_apply_launch(K, blocks, nb, N, x, out, (cudaStream_t)stream);
+  return (int)precond_apply_launch(K, blocks, false, 1.0f, nb, N, x, out, (cudaStream_t)stream);
 }
 
 // K = 16 forms

@@ -97,13 +97,18 @@ struct PrecWork {
 // once (this library's GEMM kernel, bias and tanh fused), then the blocks
 // rotated back to the lab frame and scaled.
 cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const int *nb, int N,
-                                 const float *params, float inv_a, float scale, float *blocks,
-                                 PrecWork *work, cudaStream_t stream);
-// out_i = sum_n B[n][i] x_{nb[n][i]}   (P x), 3 components per particle
-cudaError_t precond_apply_launch(int K, const float *blocks, const int *nb, int N,
-                                 const float *x, float *out, cudaStream_t stream);
-// out_{nb[n][i]} += B[n][i]^T x_i    (P^T x); out must be zeroed first
-cudaError_t precond_apply_t_launch(int K, const float *blocks, const int *nb, int N,
-                                   const float *x, float *out, cudaStream_t stream);
+                                 const float *params, float inv_a, float scale, void *blocks,
+                                 bool half, PrecWork *work, cudaStream_t stream);
+// Blocks are float, or half when `half` (then stored at unit scale and the
+// products multiply by `scale`; a float build applies its scale itself and
+// the products get 1).
+// out_i = scale sum_n B[n][i] x_{nb[n][i]}   (P x), 3 components per particle
+cudaError_t precond_apply_launch(int K, const void *blocks, bool half, float scale,
+                                 const int *nb, int N, const float *x, float *out,
+                                 cudaStream_t stream);
+// out_{nb[n][i]} += scale B[n][i]^T x_i    (P^T x); out must be zeroed first
+cudaError_t precond_apply_t_launch(int K, const void *blocks, bool half, float scale,
+                                   const int *nb, int N, const float *x, float *out,
+                                   cudaStream_t stream);
 
 }  // namespace lmg

@@ -141,8 +141,11 @@ template <class R> class Solver final : public SolverBase {
   bool prec_dirty_ = true;
   int prec_k_ = 16;  // neighbours per row of P, from the network's parameter count
   PrecLayout prec_layout_;
+  // trained with t0 = 1: M^{-1/2} scales as t0^{-1/2}
+  float prec_scale() const { return (float)(1.0 / std::sqrt(t0_)); }
   PrecWork prec_work_;
-  DeviceBuffer<float> prec_params_, prec_blocks_;
+  DeviceBuffer<float> prec_params_;
+  DeviceBuffer<uint16_t> prec_blocks_;  // P blocks in half precision, unit scale
   DeviceBuffer<int> prec_nb_;
   KnnScratch knn_scratch_;
   DeviceBuffer<R> pt_, pu_, bx_, br_, brh_, bp_, bv_, bs_, bt_;  // operator and BiCGSTAB vectors
@@ -712,12 +715,12 @@ template <class R> void Solver<R>::prec_build() {
     const int N = (int)N_;
     const int kb = prec_k_ + 1;
     int *nb = prec_nb_.ensure((size_t)N * kb);
-    float *blocks = prec_blocks_.ensure((size_t)N * kb * 9);
+    uint16_t *blocks = prec_blocks_.ensure((size_t)N * kb * 9);
     LMG_CUDA(knn_launch(prec_k_, pos_.ptr, N, batch_size(), nb, stream(), &knn_scratch_));
-    // targets were trained with t0 = 1: M^{-1/2} scales as t0^{-1/2}
+    // blocks at unit scale (the network's t0 = 1), in half precision; the
+    // products apply t0^{-1/2} (prec_scale)
     LMG_CUDA(precond_build_launch(prec_layout_, pos_.ptr, nb, N, prec_params_.ptr, (float)(1.0 / a_),
-                                  (float)(1.0 / std::sqrt(t0_)), blocks, &prec_work_,
-                                  stream()));
+                                  1.0f, blocks, true, &prec_work_, stream()));
     prec_dirty_ = false;
   }
 }
@@ -735,13 +738,13 @@ template <class R> void Solver<R>::apply_operator(const R *v, R *out) {
     R *u = pu_.ensure(n);
     const R s = (R)(1.0 / std::sqrt(r0_));  // angular part: scalar r0^{-1/2}
     LMG_CUDA(cudaMemsetAsync(t, 0, n3 * sizeof(R), stream()));
-    LMG_CUDA(precond_apply_t_launch(prec_k_, prec_blocks_.ptr, prec_nb_.ptr, N, v, t, stream()));
+    LMG_CUDA(precond_apply_t_launch(prec_k_, prec_blocks_.ptr, true, prec_scale(), prec_nb_.ptr, N, v, t, stream()));
     if (ang_) {
       scale_kernel<R><<<vec_blocks(n3), kRedThreads, 0, stream()>>>(t + n3, v + n3, n3, s);
       count_launch();
     }
     mdot_device(pos_.ptr, t, ang_ ? t + n3 : nullptr, u, ang_ ? u + n3 : nullptr);
-    LMG_CUDA(precond_apply_launch(prec_k_, prec_blocks_.ptr, prec_nb_.ptr, N, u, out, stream()));
+    LMG_CUDA(precond_apply_launch(prec_k_, prec_blocks_.ptr, true, prec_scale(), prec_nb_.ptr, N, u, out, stream()));
     if (ang_) {
       scale_kernel<R><<<vec_blocks(n3), kRedThreads, 0, stream()>>>(out + n3, u + n3, n3, s);
       count_launch();
@@ -789,7 +792,7 @@ template <class R> int Solver<R>::solve_p(const R *b, R *x) {
       bicg_p_kernel<R><<<blocks, kRedThreads, 0, st>>>(p, r, v, it == 1 ? 0.0 : beta,
                                                        omega, n);
       count_launch();
-      LMG_CUDA(precond_apply_launch(prec_k_, prec_blocks_.ptr, prec_nb_.ptr, N, p, v, st));
+      LMG_CUDA(precond_apply_launch(prec_k_, prec_blocks_.ptr, true, prec_scale(), prec_nb_.ptr, N, p, v, st));
       dot2_kernel<R><<<blocks, kRedThreads, 0, st>>>(rh, v, rh, v, n, rp, tk, out);
       count_launch();
       sync();
@@ -807,7 +810,7 @@ template <class R> int Solver<R>::solve_p(const R *b, R *x) {
         sync();
         return it;
       }
-      LMG_CUDA(precond_apply_launch(prec_k_, prec_blocks_.ptr, prec_nb_.ptr, N, s, t, st));
+      LMG_CUDA(precond_apply_launch(prec_k_, prec_blocks_.ptr, true, prec_scale(), prec_nb_.ptr, N, s, t, st));
       dot2_kernel<R><<<blocks, kRedThreads, 0, st>>>(t, s, t, t, n, rp, tk, out);
       count_launch();
       sync();
