@@ -49,6 +49,9 @@ WORKLOADS = {
     "open4k": dict(N=4096, wall=False, ang=False, tol=1e-6,
                    desc="open-boundary RPY, N=4096, forces only, phi=0.05, "
                         "Mdot + Lanczos sqrtMdotW to 1e-6"),
+    "open16k": dict(N=16384, wall=False, ang=False, tol=1e-6,
+                    desc="open-boundary RPY, N=16384, forces only, phi=0.05, "
+                         "Mdot + Lanczos sqrtMdotW to 1e-6"),
 }
 
 
@@ -285,14 +288,14 @@ def ensemble_systems(rng, nsys=256):
     return sizes, geoms, np.concatenate(pos)
 
 
-def ensemble_comparison(torch, steps, warmup, rank):
+def ensemble_comparison(torch, steps, warmup, rank, nsys=256, sequential=True):
     """Batched ensemble of 256 uneven systems (open and wall mixed) in one
     handle, FP32, tolerance 1e-6: Mdot and sqrtMdotW for all systems per call,
     against one NBody solver per system run one after the other."""
     from libmobility_gb300 import NBody
     from libmobility_gb300.ensemble import Ensemble
     rng = np.random.default_rng(4242 + rank)
-    sizes, geoms, pos = ensemble_systems(rng)
+    sizes, geoms, pos = ensemble_systems(rng, nsys)
     ntot = int(sizes.sum())
     eta = 1 / (6 * math.pi)
     f32 = dict(dtype=torch.float32, device="cuda")
@@ -337,7 +340,7 @@ def ensemble_comparison(torch, steps, warmup, rank):
     seq = []
     off = 0
     dW0 = dWs[warmup]
-    for n, gm in zip(sizes, geoms):
+    for n, gm in zip(sizes, geoms) if sequential else ():
         s = NBody("open", "open", "single_wall" if gm else "open", precision="float")
         s.setParameters(**({"wallHeight": 0.0} if gm else {}))
         s.initialize(viscosity=eta, hydrodynamicRadius=1.0, tolerance=1e-6, seed=5)
@@ -349,10 +352,10 @@ def ensemble_comparison(torch, steps, warmup, rank):
         torch.cuda.synchronize()
         seq.append(time.perf_counter() - t0)
         off += n
-    t_seq = sum(seq)
+    t_seq = sum(seq) if seq else None
     return {
-        "workload": "256 systems, N ~ U[200, 4000] (total %d), half open / half single wall "
-                    "(z ~ U[1.5, 20]), phi ~ U[0.02, 0.25], FP32, tolerance 1e-6" % ntot,
+        "workload": "%d systems, N ~ U[200, 4000] (total %d), half open / half single wall "
+                    "(z ~ U[1.5, 20]), phi ~ U[0.02, 0.25], FP32, tolerance 1e-6" % (nsys, ntot),
         "groups": len(e.describe()["groups"]),
         "setup_and_autotune_s": setup_s,
         "mdot_ms": t_mdot * 1e3,
@@ -365,8 +368,8 @@ def ensemble_comparison(torch, steps, warmup, rank):
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "what": "host time from the start of the batched call until each "
                                "system's result was known"},
-        "sequential_single_solvers_ms": t_seq * 1e3,
-        "speedup_batched_vs_sequential": t_seq / t_sqrt,
+        "sequential_single_solvers_ms": t_seq * 1e3 if t_seq else None,
+        "speedup_batched_vs_sequential": t_seq / t_sqrt if t_seq else None,
     }
 
 
@@ -610,9 +613,19 @@ def main():
                     help="skip the batched ensemble of 256 uneven systems")
     ap.add_argument("--skip-large", action="store_true",
                     help="skip the N = 262144 single-wall Mdot")
+    ap.add_argument("--only", choices=["ensemble"], default=None,
+                    help="run one sub-measurement alone and print it (for profiling)")
+    ap.add_argument("--ensemble-systems", type=int, default=256)
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     ws, rank, local = dist_setup()
+    if args.only == "ensemble":  # the ensemble measurement alone (profiling runs)
+        import torch
+        out = ensemble_comparison(torch, args.steps, args.warmup, rank, args.ensemble_systems,
+                                  sequential=False)
+        if rank == 0:
+            print(json.dumps({"ensemble": out}))
+        return
     if args.impl == "reference":
         run_reference(args, w, ws, rank)
     else:

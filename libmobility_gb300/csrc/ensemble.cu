@@ -234,8 +234,17 @@ __global__ void ens_estimate(const R *V, size_t ldv, int m, const double *coef, 
   const int o = off3[s], n = nn[s];
   double v[2] = {0.0, 0.0};
   for (int e = threadIdx.x; e < n; e += kEnsThreads) {
-    R acc = 0;
-    for (int k = 0; k < m; k++) acc += cs[k] * V[(size_t)k * ldv + o + e];
+    // eight independent partial sums: eight basis-vector loads in flight
+    R part[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const R *col = V + o + e;
+    int k = 0;
+    for (; k + 8 <= m; k += 8) {
+#pragma unroll
+      for (int u = 0; u < 8; u++) part[u] += cs[k + u] * col[(size_t)(k + u) * ldv];
+    }
+    for (; k < m; k++) part[k & 7] += cs[k] * col[(size_t)k * ldv];
+    const R acc = ((part[0] + part[1]) + (part[2] + part[3])) +
+                  ((part[4] + part[5]) + (part[6] + part[7]));
     ynew[o + e] = acc;
     const double a = (double)yold[o + e], d = (double)acc - a;
     v[0] += a * a;
