@@ -199,16 +199,15 @@ mdot_kernel(const MdotArgs<R> a) {
   constexpr int NC = ANG ? 6 : 3;  // accumulated components per target
   constexpr bool COMP = sizeof(R) == 4;  // compensated accumulation in FP32
 
-  // The fused FP32 wall evaluation (all blocks) and the FP32 open UF
-  // evaluation take two sources at a time in packed f32x2 instructions
-  // (pack2.cuh); their sources are staged as separate arrays (x, y, z, F,
-  // and T for the wall) so that one float4 read yields a component of four
-  // sources.
+  // The fused FP32 wall evaluation (all blocks) and the FP32 forces-only
+  // evaluations (open and wall UF) take two sources at a time in packed f32x2
+  // instructions (pack2.cuh); their sources are staged as separate arrays
+  // (x, y, z, F, and T for all blocks) so that one float4 read yields a
+  // component of four sources.
   constexpr bool PACK = PK::FUSED_WALL;
-  constexpr bool PACK_OPEN =
-      GEOM == kOpen && sizeof(R) == 4 && HAS_F && !ANG && THREADS % 32 == 0;
-  constexpr int NSV = PACK ? 9 : (PACK_OPEN ? 6 : 1);
-  constexpr bool SOA = PACK || PACK_OPEN;
+  constexpr bool PACK_UF = sizeof(R) == 4 && HAS_F && !ANG && THREADS % 32 == 0;
+  constexpr int NSV = PACK ? 9 : (PACK_UF ? 6 : 1);
+  constexpr bool SOA = PACK || PACK_UF;
   __shared__ Q4<R> sp[SOA ? 1 : THREADS];
   __shared__ Q4<R> sf[HAS_F && !SOA ? THREADS : 1];
   __shared__ Q4<R> st[USE_T && !SOA ? THREADS : 1];
@@ -344,7 +343,45 @@ mdot_kernel(const MdotArgs<R> a) {
                               u[t], w[t]);
         }
       }
-    } else if constexpr (PACK_OPEN) {
+    } else if constexpr (PACK_UF && GEOM == kWall) {
+      if (uniform && n_here == THREADS) {
+        // two sources per instruction; close pairs fall back lane by lane
+        V3p u2[TPT];
+#pragma unroll
+        for (int t = 0; t < TPT; t++) u2[t] = {bc(0.f), bc(0.f), bc(0.f)};
+#pragma unroll 1
+        for (int jj = 0; jj < THREADS; jj += 4) {
+          float4 q[6];
+#pragma unroll
+          for (int c = 0; c < 6; c++) q[c] = *reinterpret_cast<const float4 *>(&sv[c][jj]);
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            F2 v[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) v[c] = h ? mk2(q[c].z, q[c].w) : mk2(q[c].x, q[c].y);
+#pragma unroll
+            for (int t = 0; t < TPT; t++)
+              wall_uf_pair_x2(a.k, a.kw, bc(xi[t]), bc(yi[t]), bc(zi[t]), v[0], v[1], v[2],
+                              v[3], v[4], v[5], u2[t]);
+          }
+        }
+#pragma unroll
+        for (int t = 0; t < TPT; t++) {  // the two lanes hold even and odd sources
+          u[t].x += u2[t].x.v.x + u2[t].x.v.y;
+          u[t].y += u2[t].y.v.x + u2[t].y.v.y;
+          u[t].z += u2[t].z.v.x + u2[t].z.v.y;
+        }
+      } else {
+        for (int jj = 0; jj < n_here; jj++) {
+          const int j = ts + jj;
+          const Q4<R> p = {sv[0][jj], sv[1][jj], sv[2][jj], 0};
+          const Q4<R> fv = {sv[3][jj], sv[4][jj], sv[5][jj], 0};
+#pragma unroll
+          for (int t = 0; t < TPT; t++)
+            if (j >= lo[t] && j < hi[t]) PK::eval(a.k, a.kw, xi[t], yi[t], zi[t], p, fv, fv, u[t], w[t]);
+        }
+      }
+    } else if constexpr (PACK_UF) {
       if (uniform && n_here == THREADS) {
         // as the scalar full-tile path below, two sources per instruction
 #pragma unroll 1

@@ -137,6 +137,59 @@ __device__ __forceinline__ void wall_pair_fused_x2(
   u.z = fms2(k1, fma2(dy, Tx, neg2(dx * Ty)), fma2(mp, ez, fma2(pv, f2i, u.z)));
 }
 
+// Packed wall UF pair (forces only): the translational part of
+// wall_pair_fused_x2 above (RPY UF merged with the translational image C2),
+// same formulas and order of operations.  Pairs closer than 2a in either lane
+// (the self pair included) are evaluated lane by lane with the scalar
+// wall_pair_fused with zero torques, keeping its u.
+__device__ __forceinline__ void wall_uf_pair_x2(const PairConst<float> &k, const WallConst &K,
+                                                F2 xi, F2 yi, F2 hi, F2 Xj, F2 Yj, F2 Hj,
+                                                F2 Fx, F2 Fy, F2 Fz, V3p &u) {
+  const F2 dx = xi - Xj, dy = yi - Yj, dz = hi - Hj;
+  const F2 sxy = fma2(dx, dx, dy * dy);
+  const F2 r2 = fma2(dz, dz, sxy);
+  if (r2.v.x < 4.0f || r2.v.y < 4.0f) {
+    Vec3<float> u0 = {0, 0, 0}, w0 = {0, 0, 0}, u1 = {0, 0, 0}, w1 = {0, 0, 0};
+    wall_pair_fused(k, K, xi.v.x, yi.v.x, hi.v.x, Xj.v.x, Yj.v.x, Hj.v.x, Fx.v.x, Fy.v.x,
+                    Fz.v.x, 0.f, 0.f, 0.f, u0, w0);
+    wall_pair_fused(k, K, xi.v.y, yi.v.y, hi.v.y, Xj.v.y, Yj.v.y, Hj.v.y, Fx.v.y, Fy.v.y,
+                    Fz.v.y, 0.f, 0.f, 0.f, u1, w1);
+    u.x = u.x + mk2(u0.x, u1.x);
+    u.y = u.y + mk2(u0.y, u1.y);
+    u.z = u.z + mk2(u0.z, u1.z);
+    return;
+  }
+  const F2 Rz = hi + Hj;
+  const F2 ir = rsq2(r2);
+  const F2 ir2 = ir * ir;
+  const F2 ir3 = ir2 * ir;
+  const F2 f = ir * fma2(bc(k.tf1), ir2, bc(k.tf0));
+  const F2 G = ir3 * fma2(bc(k.tg1), ir2, bc(k.tg0));
+  const F2 iR = rsq2(fma2(Rz, Rz, sxy));
+  const F2 ex = dx * iR, ey = dy * iR, ez = Rz * iR;
+  const F2 hhj = Hj * rcp2(Rz);
+  const F2 q = ez * ez;
+  const F2 iR2 = iR * iR, iR3 = iR2 * iR, iR5 = iR3 * iR2;
+  const F2 h1q = fms2(hhj, hhj, hhj) * q;
+  const F2 A = fma2(iR, fma2(bc(K.a11), h1q, bc(K.a10)),
+                    fma2(iR3, fma2(bc(K.a31), q, bc(K.a30)), iR5 * fma2(bc(K.a51), q, bc(K.a50))));
+  const F2 B = fma2(iR, fma2(bc(K.b11), h1q, bc(K.b10)),
+                    fma2(iR3, fma2(bc(K.b31), q, bc(K.b30)), iR5 * fma2(bc(K.b51), q, bc(K.b50))));
+  const F2 C = ez * fma2(iR, fma2(bc(K.c1h), hhj, bc(K.c11) * h1q),
+                         fma2(iR3, fma2(bc(K.c31), q, bc(K.c30)),
+                              iR5 * fma2(bc(K.c51), q, bc(K.c50))));
+  const F2 D = ez * fma2(bc(K.d1) * hhj, iR, bc(K.d5) * iR5);
+  const F2 E = fma2(bc(K.e1) * q, fma2(hhj * hhj, iR, iR3), iR5 * fma2(bc(K.e51), q, bc(K.e50)));
+  const F2 ev = fma2(ex, Fx, fma2(ey, Fy, ez * Fz));
+  const F2 dF = fma2(dx, Fx, fma2(dy, Fy, dz * Fz));
+  const F2 fA = f + A;
+  const F2 g = G * dF;
+  const F2 s = fma2(B, ev, C * Fz);
+  u.x = fma2(fA, Fx, fma2(g, dx, fma2(s, ex, u.x)));
+  u.y = fma2(fA, Fy, fma2(g, dy, fma2(s, ey, u.y)));
+  u.z = fma2(fA, Fz, fma2(g, dz, fma2(s, ez, fma2(D, ev, fma2(E, Fz, u.z)))));
+}
+
 // Packed open-space UF pair (translational RPY, forces only) in the fast
 // form of PairKernel::eval<false> (mdot.cuh): r^2 clamped at 4 for the
 // coefficients, so overlapping and self pairs give finite values that the
