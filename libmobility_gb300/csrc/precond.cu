@@ -205,7 +205,7 @@ knn_search_kernel(int N, KnnGridShape g, const int *__restrict__ start,
 
 cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaStream_t stream,
                        KnnScratch *scratch) {
-  if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
+  if (K != 16 && K != 32 && K != 48 && K != 64) return cudaErrorInvalidValue;
   if (N <= 0) return cudaSuccess;
   KnnScratch local;
   KnnScratch &w = scratch ? *scratch : local;
@@ -279,6 +279,7 @@ cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaSt
   if (K == 16) knn_search_kernel<17><<<sg, kSearchThreads, 0, stream>>>(N, g, start, sidx, spos, nb);
   if (K == 32) knn_search_kernel<33><<<sg, kSearchThreads, 0, stream>>>(N, g, start, sidx, spos, nb);
   if (K == 48) knn_search_kernel<49><<<sg, kSearchThreads, 0, stream>>>(N, g, start, sidx, spos, nb);
+  if (K == 64) knn_search_kernel<65><<<sg, kSearchThreads, 0, stream>>>(N, g, start, sidx, spos, nb);
   e = cudaGetLastError();
   if (e == cudaSuccess && !scratch) e = cudaStreamSynchronize(stream);  // before `local` goes
   return e;
@@ -414,7 +415,7 @@ cudaError_t gemm_launch(int ta, int tb, int M, int N, int K, const float *A, int
 cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const int *nb, int N,
                                  const float *params, float inv_a, float scale, void *blocks,
                                  bool half, PrecWork *work, cudaStream_t stream) {
-  if (L.K != 16 && L.K != 32 && L.K != 48) return cudaErrorInvalidValue;
+  if (L.K != 16 && L.K != 32 && L.K != 48 && L.K != 64) return cudaErrorInvalidValue;
   if (N <= 0) return cudaSuccess;
   PrecWork local;
   PrecWork &w = work ? *work : local;
@@ -429,6 +430,7 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
   if (L.K == 16) precond_features_kernel<16><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
   if (L.K == 32) precond_features_kernel<32><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
   if (L.K == 48) precond_features_kernel<48><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
+  if (L.K == 64) precond_features_kernel<64><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
     e = gemm_launch(0, 0, N, L.H, L.In, X, L.In, params + L.W1, L.H, H1, L.H, params + L.B1, 1,
@@ -449,9 +451,11 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
   if (L.K == 16 && half) precond_assemble_kernel<16><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bh);
   if (L.K == 32 && half) precond_assemble_kernel<32><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bh);
   if (L.K == 48 && half) precond_assemble_kernel<48><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bh);
+  if (L.K == 64 && half) precond_assemble_kernel<64><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bh);
   if (L.K == 16 && !half) precond_assemble_kernel<16><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bf);
   if (L.K == 32 && !half) precond_assemble_kernel<32><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bf);
   if (L.K == 48 && !half) precond_assemble_kernel<48><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bf);
+  if (L.K == 64 && !half) precond_assemble_kernel<64><<<ga, 256, 0, stream>>>(Y, E, N, ym, ys, scale, bf);
   e = cudaGetLastError();
   if (e == cudaSuccess && !work) e = cudaStreamSynchronize(stream);  // before `local` goes
   return e;
@@ -533,11 +537,12 @@ template <class T>
 cudaError_t apply_k(int K, bool transpose, const void *blocks, const int *nb, int N,
                     const float *x, float *out, float scale, cudaStream_t stream) {
   const T *B = static_cast<const T *>(blocks);
-  if (K != 16 && K != 32 && K != 48) return cudaErrorInvalidValue;
+  if (K != 16 && K != 32 && K != 48 && K != 64) return cudaErrorInvalidValue;
   count_launch();
   if (K == 16) apply_dispatch<17, T>(transpose, B, nb, N, x, out, scale, stream);
   if (K == 32) apply_dispatch<33, T>(transpose, B, nb, N, x, out, scale, stream);
   if (K == 48) apply_dispatch<49, T>(transpose, B, nb, N, x, out, scale, stream);
+  if (K == 64) apply_dispatch<65, T>(transpose, B, nb, N, x, out, scale, stream);
   return cudaGetLastError();
 }
 

@@ -6,7 +6,7 @@
 // so P only changes the cost, never the statistics.
 //
 // P here is sparse: row block i holds 3x3 blocks for particle i and its K
-// nearest neighbours (K = 16, 32 or 48, fixed by the network), approximating
+// nearest neighbours (K = 16, 32, 48 or 64, fixed by the network), approximating
 // row i of the inverse square root of the mobility of that (K+1)-particle
 // neighbourhood.  (A block-diagonal P cannot help
 // the RPY mobility: its diagonal blocks of M^{-1/2} are nearly scalar; the
@@ -29,7 +29,7 @@
 
 namespace lmg {
 
-// Network shape for K neighbours (16, 32 or 48) and hidden width H (64, 128,
+// Network shape for K neighbours (16, 32, 48 or 64) and hidden width H (64, 128,
 // 256 or 512): parameters and normalisation, FP32, in one contiguous array:
 //   W1[3K][H] b1[H] W2[H][H] b2[H] W3[H][6+9K] b3[6+9K]
 //   xmean[3K] xstd[3K] ymean[6+9K] ystd[6+9K]
@@ -62,7 +62,7 @@ inline PrecLayout prec_layout(int K, int H) {
 
 // The layout whose parameter count is n (K = 0 if there is none).
 inline PrecLayout prec_layout_for_params(size_t n) {
-  for (int K : {16, 32, 48})
+  for (int K : {16, 32, 48, 64})
     for (int H : {64, 128, 256, 512}) {
       const PrecLayout L = prec_layout(K, H);
       if ((size_t)L.Params == n) return L;
@@ -70,7 +70,7 @@ inline PrecLayout prec_layout_for_params(size_t n) {
   return PrecLayout{};
 }
 
-// Launchers (precond.cu) for K = 16, 32 or 48.  All pointers are device
+// Launchers (precond.cu) for K = 16, 32, 48 or 64.  All pointers are device
 // memory; all work goes on `stream`.  Layouts, stored so that consecutive
 // particles are consecutive in memory: nb[n][i] (n = 0 the particle itself,
 // then its K nearest in distance order), blocks[n][e][i] (element e = 3 r + c

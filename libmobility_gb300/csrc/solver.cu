@@ -693,7 +693,7 @@ void Solver<R>::set_preconditioner(const std::string &kind, const float *params,
   if (L.K == 0)
     throw Error(LMG_ERR_INVALID_ARGUMENT,
                 "[libmobility_gb300] preconditioner parameters: " + std::to_string(n) +
-                    " floats is not the size of a network over K = 16, 32 or 48 neighbours "
+                    " floats is not the size of a network over K = 16, 32, 48 or 64 neighbours "
                     "with 64, 128, 256 or 512 hidden units");
   float *d = prec_params_.ensure(n);
   LMG_CUDA(cudaMemcpy(d, params, n * sizeof(float), cudaMemcpyHostToDevice));

@@ -26,7 +26,7 @@ NIN, NOUT = 3 * K, 6 + 9 * K
 
 def kh_of(flat):
     """(neighbours, hidden units) of a flat parameter vector."""
-    for k in (16, 32, 48):
+    for k in (16, 32, 48, 64):
         for h in (64, 128, 256, 512):
             if len(flat) == sum(int(np.prod(s)) for _, s in shapes(k, h)):
                 return k, h
