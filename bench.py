@@ -54,6 +54,12 @@ WORKLOADS = {
                          "Mdot + Lanczos sqrtMdotW to 1e-6"),
 }
 
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the Mdot kernel
+# from one ncu capture of each workload (profiles/mdot_kernel_*.md); the
+# kernel reads its inputs once (positions, forces, torques) and writes the
+# split partials, which stay in L2
+MDOT_TRAFFIC = {"wall16k": 633.3e3, "open16k": 417.8e3}
+
 
 def make_inputs(w, seed):
     rng = np.random.default_rng(seed)
@@ -407,6 +413,54 @@ def large_wall_mdot(torch, rank, reps=3):
             "achieved_tflops": pairs * FLOPS_PER_PAIR[("wall", True)] / t / 1e12}
 
 
+def hbm_peak_gbs():
+    """The measured copy bandwidth (GB/s), None when the file is absent."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                               "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def krylov_phases(torch, s, ddW, t_mdot, solves=3):
+    """Device time of the Lanczos work outside the matvec on the main
+    workload: the vector updates after each matvec (alpha, beta, next basis
+    vector: 4 n s algorithmic bytes per iteration) and the convergence checks
+    (y = |z| V c over m basis vectors, (m + 1) n s, plus 2 n s for the error
+    norm), against the measured HBM copy bandwidth.  The vectors are n = 6N
+    FP32 (393 KB at N = 16384): they live in L2 and each update is a few
+    launches of a grid reduction, so these phases are latency-bound."""
+    torch.cuda.synchronize()
+    s._lanczos_phase_timing(True)
+    for _ in range(solves):
+        s.sqrtMdotW_noise(ddW)
+    torch.cuda.synchronize()
+    t = s._lanczos_phase_times()
+    s._lanczos_phase_timing(False)
+    its = t["iterations"] / t["solves"]
+    peak = hbm_peak_gbs()
+    vec_gbs = t["vector_bytes"] / (t["vector_ms"] * 1e-3) / 1e9
+    chk_gbs = t["check_bytes"] / (t["check_ms"] * 1e-3) / 1e9
+    return {
+        "solves": int(t["solves"]),
+        "iterations_issued_per_solve": its,
+        "checks_per_solve": t["checks"] / t["solves"],
+        "vector_update_us_per_iteration": 1e3 * t["vector_ms"] / t["iterations"],
+        "vector_update_bytes_per_iteration": t["vector_bytes"] / t["iterations"],
+        "vector_update_gbs": vec_gbs,
+        "check_us_per_check": 1e3 * t["check_ms"] / max(1, t["checks"]),
+        "check_gbs": chk_gbs,
+        "hbm_peak_gbs": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy)",
+        "vector_update_frac": vec_gbs / peak if peak else None,
+        "check_frac": chk_gbs / peak if peak else None,
+        "matvec_us": t_mdot * 1e6,
+        "vector_share_of_iteration": (t["vector_ms"] / t["iterations"])
+        / (t["vector_ms"] / t["iterations"] + t_mdot * 1e3),
+        "note": "checks run on a high-priority side stream, overlapping the next matvec",
+    }
+
+
 def cpu_baseline(w, pos, F, T, seconds=8.0):
     """FP64 C oracle (all host threads) on a bounded sample of the workload:
     the first R target rows against every source."""
@@ -520,6 +574,7 @@ def run_ours(args, w, ws, rank, local):
         s.sqrtMdotW_noise(ddW)
     torch.cuda.synchronize()
     t_sqrt = (time.perf_counter() - t0) / 3
+    krylov = krylov_phases(torch, s, ddW, t_mdot)
     peak = fp32_peak_tflops(lib, torch)
     fpp = FLOPS_PER_PAIR[("wall" if w["wall"] else "open", w["ang"])]
     achieved = pairs * fpp / t_mdot / 1e12
@@ -584,12 +639,15 @@ def run_ours(args, w, ws, rank, local):
         "sqrtMdotW_learned_vs_plain": cmp,
         "ensemble_256": ens,
         "wall_262k_mdot": large,
+        "krylov_phases": krylov,
         "mdot_pair_interactions_per_s": pairs / t_mdot,
         "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e * 1e3},
         "roofline": {"bound": "fp32", "kernel": "mdot_kernel (pair interactions)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": MDOT_TRAFFIC.get(args.workload),
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "ncu capture of this kernel and workload",
                      "peak_source": "FP32 FMA-chain probe measured in this run",
                      "flops_per_pair": fpp, "kernel_ms": t_mdot * 1e3,
                      "kernel_timing": kernel_timing},

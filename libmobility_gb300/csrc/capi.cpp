@@ -216,6 +216,23 @@ int lmg_internal_tridiag_sqrt_e1(const double *alpha, const double *beta, int m,
   return lmg::tridiag_sqrt_e1_host(alpha, beta, m, out);
 }
 
+// Internal measurement hooks (not part of the public header): switch the
+// Lanczos phase timing on or off (either resets the sums), and read the sums
+// as out[7] = {vector_ms, vector_bytes, check_ms, check_bytes, iterations,
+// checks, solves}.
+int lmg_internal_lanczos_phase_timing(lmg_solver *h, int on) {
+  return guarded(h, [&](lmg::SolverBase &m) { m.set_phase_timing(on != 0); });
+}
+
+int lmg_internal_lanczos_phase_times(lmg_solver *h, double *out) {
+  if (!h || !h->impl || !out) return LMG_ERR_INVALID_ARGUMENT;
+  const auto &p = h->impl->phase_times();
+  const double v[7] = {p.vector_ms, p.vector_bytes, p.check_ms, p.check_bytes,
+                       (double)p.iterations, (double)p.checks, (double)p.solves};
+  for (int q = 0; q < 7; q++) out[q] = v[q];
+  return LMG_OK;
+}
+
 
 lmg_status lmg_ensemble_create(int precision, lmg_ensemble **out) {
   if (!out) return LMG_ERR_INVALID_ARGUMENT;

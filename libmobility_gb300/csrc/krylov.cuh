@@ -186,55 +186,103 @@ __global__ void krylov_scale_first_kernel(const R *z, R *v0, size_t n, const Kry
     v0[e] = z[e] * inv;
 }
 
-// w -= beta_{i-1} v_{i-1};  alpha_i = w . v_i
-template <class R>
-__global__ void krylov_alpha_kernel(R *w, const R *vi, const R *vprev, size_t n, int i,
-                                    double *partials, unsigned *ticket, KrylovScalars *sc) {
-  const R bprev = i > 0 ? (R)sc->beta[i - 1] : R(0);
-  double v[1] = {0.0};
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x) {
-    R x = w[e];
-    if (i > 0) x -= bprev * vprev[e];
-    w[e] = x;
-    v[0] += (double)x * (double)vi[e];
+// ---------------------------------------------------------------------------
+// The vector work of one Lanczos iteration after the matvec, in one
+// cooperative launch (all blocks resident) with grid barriers between its
+// three phases, each a grid-stride pass with an FP64 block-ordered reduction:
+//   w -= beta_{i-1} v_{i-1};  alpha_i = w . v_i
+//   w -= alpha_i v_i;  beta_i = |w|, zeroed below 1e-3 alpha_i/|z|
+//   v_{i+1} = w / beta_i, or e1 after a breakdown
+// (one launch instead of three saves two launch gaps per iteration).  Each
+// barrier wait is bounded (~1 s): a block that gives up raises err_flag
+// (mapped host memory, read by the host at its next check) and returns; the
+// host resets the barrier words before every solve.
+// ---------------------------------------------------------------------------
+constexpr long kBarrierSpins = 1L << 24;  // x >= 64 ns sleep: > 1 s
+
+// bar[0] arrivals, bar[1] generation.  Returns false if the wait ran out.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      ok = 0;
+      for (long it = 0; it < kBarrierSpins; it++) {
+        if (*gen != g) {
+          ok = 1;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok;
   }
-  double tot[1];
-  if (grid_sum<1>(v, partials, ticket, tot)) sc->alpha[i] = tot[0];
+  __syncthreads();
+  return s_ok != 0;
 }
 
-// w -= alpha_i v_i;  beta_i = |w| with the breakdown rule
 template <class R>
-__global__ void krylov_beta_kernel(R *w, const R *vi, size_t n, int i, double *partials,
-                                   unsigned *ticket, KrylovScalars *sc, double *host_ab) {
-  const R al = (R)sc->alpha[i];
-  double v[1] = {0.0};
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const R x = w[e] - al * vi[e];
-    w[e] = x;
-    v[0] += (double)x * (double)x;
+__global__ void __launch_bounds__(kRedThreads)
+krylov_step_kernel(R *w, const R *vi, const R *vprev, R *vnext, size_t n, int i,
+                   double *partials, unsigned *ticket, unsigned *bar, KrylovScalars *sc,
+                   double *host_ab, double *err_flag) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t e0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  // w -= beta_{i-1} v_{i-1};  alpha_i = w . v_i
+  {
+    const R bprev = i > 0 ? (R)sc->beta[i - 1] : R(0);
+    double v[1] = {0.0};
+    for (size_t e = e0; e < n; e += stride) {
+      R x = w[e];
+      if (i > 0) x -= bprev * vprev[e];
+      w[e] = x;
+      v[0] += (double)x * (double)vi[e];
+    }
+    double tot[1];
+    if (grid_sum<1>(v, partials, ticket, tot)) sc->alpha[i] = tot[0];
   }
-  double tot[1];
-  if (grid_sum<1>(v, partials, ticket, tot)) {
-    double b = sqrt(tot[0]);
-    const double tol = 1e-3 * sc->alpha[i] / sc->normz;  // LanczosAlgorithm.cu:141-143
-    if (b < tol) b = 0.0;
-    sc->beta[i] = b;
-    // (alpha_i, beta_i) for the host-side eigen-solve, in mapped host memory
-    host_ab[2 * i] = sc->alpha[i];
-    host_ab[2 * i + 1] = b;
+  if (!grid_barrier(bar)) {
+    *err_flag = 1.0;
+    return;
   }
-}
-
-// v_{i+1} = w / beta_i, or e1 after a breakdown (LanczosAlgorithm.cu:144-152)
-template <class R>
-__global__ void krylov_next_kernel(const R *w, R *vnext, size_t n, int i, const KrylovScalars *sc) {
-  const double b = sc->beta[i];
+  // w -= alpha_i v_i;  beta_i = |w| with the breakdown rule
+  {
+    const R al = (R)__ldcg(&sc->alpha[i]);
+    double v[1] = {0.0};
+    for (size_t e = e0; e < n; e += stride) {
+      const R x = w[e] - al * vi[e];
+      w[e] = x;
+      v[0] += (double)x * (double)x;
+    }
+    double tot[1];
+    if (grid_sum<1>(v, partials, ticket, tot)) {
+      double b = sqrt(tot[0]);
+      const double a = __ldcg(&sc->alpha[i]);
+      const double tol = 1e-3 * a / sc->normz;  // LanczosAlgorithm.cu:141-143
+      if (b < tol) b = 0.0;
+      sc->beta[i] = b;
+      host_ab[2 * i] = a;
+      host_ab[2 * i + 1] = b;
+    }
+  }
+  if (!grid_barrier(bar)) {
+    *err_flag = 1.0;
+    return;
+  }
+  // v_{i+1} = w / beta_i, or e1 after a breakdown
+  const double b = __ldcg(&sc->beta[i]);
   const R inv = b > 0.0 ? (R)(1.0 / b) : R(0);
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x)
-    vnext[e] = b > 0.0 ? w[e] * inv : (e == 0 ? R(1) : R(0));
+  for (size_t e = e0; e < n; e += stride)
+    vnext[e] = b > 0.0 ? __ldcg(w + e) * inv : (e == 0 ? R(1) : R(0));
 }
 
 // ---------------------------------------------------------------------------

@@ -3,12 +3,15 @@
 //     state how many of its kernels ran inside a timed region;
 //   * an FP32 FMA-chain kernel whose throughput is the FP32 peak the pair
 //     kernel's roofline is quoted against (measured on the same GPU, same
-//     clocks, in the same run).
+//     clocks, in the same run);
+//   * a check that the bounded grid barrier of the fused Lanczos step gives
+//     up and reports instead of waiting forever.
 #include <atomic>
 #include <cstdint>
 
 #include <cuda_runtime.h>
 
+#include "krylov.cuh"
 #include "launch_count.hpp"
 
 namespace lmg {
@@ -56,6 +59,13 @@ __global__ void fma2_chain_kernel(int iters, float *sink) {
   for (int k = 0; k < 4; k++) s += a[k].x + a[k].y;
   if (s == -1.0f) sink[threadIdx.x] = s;
 }
+
+// Two blocks meet at a barrier whose arrival count starts at 7: neither is
+// the last arrival, nothing advances the generation word, so both waits run
+// out and report.
+__global__ void barrier_timeout_kernel(unsigned *bar, double *flag) {
+  if (!lmg::grid_barrier(bar) && threadIdx.x == 0) flag[blockIdx.x] = 1.0;
+}
 }  // namespace
 
 extern "C" {
@@ -83,5 +93,31 @@ int lmg_internal_fma_probe(int blocks, int threads, int iters, void *sink, void 
 int lmg_internal_fma2_probe(int blocks, int threads, int iters, void *sink, void *stream) {
   fma2_chain_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, (float *)sink);
   return (int)cudaGetLastError();
+}
+
+// Runs barrier_timeout_kernel (about 1-2 s) and returns in *gave_up the
+// number of blocks whose wait ran out (2 expected); the return value is the
+// CUDA status, so the context is shown usable afterwards.
+int lmg_internal_barrier_timeout_probe(int *gave_up) {
+  if (!gave_up) return 1;
+  *gave_up = -1;
+  unsigned *bar = nullptr;
+  double *flag = nullptr;
+  cudaError_t e = cudaMalloc(&bar, 2 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&flag, 2 * sizeof(double));
+  const unsigned init[2] = {7u, 0u};
+  if (e == cudaSuccess) e = cudaMemcpy(bar, init, sizeof(init), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(flag, 0, 2 * sizeof(double));
+  if (e == cudaSuccess) {
+    barrier_timeout_kernel<<<2, 32>>>(bar, flag);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  double h[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, flag, sizeof(h), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) *gave_up = (int)(h[0] + h[1]);
+  if (bar) cudaFree(bar);
+  if (flag) cudaFree(flag);
+  return (int)e;
 }
 }

@@ -98,6 +98,8 @@ template <class R> class Solver final : public SolverBase {
       if (e) cudaEventDestroy(e);
     if (ev_check_) cudaEventDestroy(ev_check_);
     if (ev_side_) cudaEventDestroy(ev_side_);
+    for (auto &e : ev_phase_)
+      if (e) cudaEventDestroy(e);
     if (side_) cudaStreamDestroy(side_);
   }
 
@@ -134,6 +136,9 @@ template <class R> class Solver final : public SolverBase {
   PinnedBuffer<double> h_dbl_;
   cudaStream_t side_ = nullptr;       // high-priority stream for per-check work
   cudaEvent_t ev_iter_[2] = {nullptr, nullptr}, ev_check_ = nullptr, ev_side_ = nullptr;
+  // phase timing: per iteration j, [4j, 4j+1] bracket the vector updates and
+  // [4j+2, 4j+3] the check (created on the first timed solve)
+  std::vector<cudaEvent_t> ev_phase_;
   // RFD
   DeviceBuffer<R> rfd_noise_, rfd_pos_, rfd_mp_, rfd_mm_;
   // learned preconditioner
@@ -150,6 +155,7 @@ template <class R> class Solver final : public SolverBase {
   KnnScratch knn_scratch_;
   DeviceBuffer<R> pt_, pu_, bx_, br_, brh_, bp_, bv_, bs_, bt_;  // operator and BiCGSTAB vectors
   int num_sms_ = 0;
+  int step_per_sm_ = 0;  // resident krylov_step_kernel blocks per SM
   bool tickets_zeroed_ = false;
   std::map<long, MdotPlan> plans_;
 
@@ -196,8 +202,10 @@ template <class R> void Solver<R>::ensure_reduction(int blocks) {
   // two halves: the solver stream and the side stream reduce independently
   red_part_.ensure((size_t)8 * std::max(blocks, 1024));
   if (!red_ticket_.ptr) {
-    red_ticket_.ensure(4);
-    LMG_CUDA(cudaMemsetAsync(red_ticket_.ptr, 0, 4 * sizeof(unsigned), stream()));
+    // [0] solver-stream ticket, [1] side-stream ticket, [3] min ticket,
+    // [4..5] grid barrier of the fused Lanczos step
+    red_ticket_.ensure(8);
+    LMG_CUDA(cudaMemsetAsync(red_ticket_.ptr, 0, 8 * sizeof(unsigned), stream()));
   }
 }
 
@@ -407,9 +415,23 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
   RotLog log{rot_cs_.data(), rot_idx_.data(), rot_cap};
   cudaStream_t st = stream();
   cudaStream_t sd = side_;
-  unsigned *tk = red_ticket_.ptr, *tk_side = red_ticket_.ptr + 1;
+  unsigned *tk = red_ticket_.ptr, *tk_side = red_ticket_.ptr + 1, *bar = red_ticket_.ptr + 4;
   double *rp = red_part_.ptr, *rp_side = red_part_.ptr + red_half();
   const size_t n3 = 3 * (size_t)N_;
+  // the fused vector step is a cooperative launch: every block resident
+  if (!step_per_sm_) {
+    LMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&step_per_sm_, krylov_step_kernel<R>,
+                                                           kRedThreads, 0));
+    if (step_per_sm_ < 1)
+      throw Error(LMG_ERR_INTERNAL, "[libmobility_gb300] Lanczos step kernel cannot be resident");
+  }
+  const int step_blocks = std::min(blocks, step_per_sm_ * sms());
+  double *err_flag = mir_dev + 516;
+  mir[516] = 0.0;
+  // the tickets and barrier words return to zero after every reduction and
+  // barrier; a barrier that timed out leaves them inconsistent, so every
+  // solve starts from zero (the side stream's last work precedes this point)
+  LMG_CUDA(cudaMemsetAsync(red_ticket_.ptr, 0, 6 * sizeof(unsigned), st));
 
   LMG_CUDA(cudaMemsetAsync(sc, 0, sizeof(KrylovScalars), st));
   krylov_norm_kernel<R><<<blocks, kRedThreads, 0, st>>>(z, n, rp, tk, sc);
@@ -417,17 +439,28 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
   krylov_scale_first_kernel<R><<<blocks, kRedThreads, 0, st>>>(z, V, n, sc);
   count_launch();
 
+  if (timing_ && ev_phase_.empty()) {
+    ev_phase_.assign(4 * (kMaxLanczosIterations + 1), nullptr);
+    for (auto &e : ev_phase_) LMG_CUDA(cudaEventCreate(&e));
+  }
+  int issued = 0;
+  std::vector<int> checked;
   auto issue = [&](int j) {
     R *vj = V + (size_t)j * n;
     apply_operator(vj, w);
-    krylov_alpha_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vj, j > 0 ? vj - n : vj, n, j, rp,
-                                                           tk, sc);
+    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[4 * j], st));
+    const R *vprev = j > 0 ? vj - n : vj;
+    R *vnext = vj + n;
+    size_t nn = n;
+    int jj = j;
+    void *args[] = {&w, (void *)&vj, (void *)&vprev, &vnext, &nn, &jj, &rp, &tk, &bar,
+                    &sc, &mir_dev, &err_flag};
+    LMG_CUDA(cudaLaunchCooperativeKernel((const void *)krylov_step_kernel<R>, dim3(step_blocks),
+                                         dim3(kRedThreads), args, 0, st));
     count_launch();
-    krylov_beta_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vj, n, j, rp, tk, sc, mir_dev);
-    count_launch();
-    krylov_next_kernel<R><<<blocks, kRedThreads, 0, st>>>(w, vj + n, n, j, sc);
-    count_launch();
+    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[4 * j + 1], st));
     LMG_CUDA(cudaEventRecord(ev_iter_[j & 1], st));
+    issued = j + 1;
   };
 
   const int k = std::min(check_steps_, limit - 2);
@@ -441,6 +474,8 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     if (!(i >= k || cb_ != nullptr)) continue;
     const int m = i + 1;
     LMG_CUDA(cudaEventSynchronize(ev_iter_[i & 1]));
+    if (mir[516] != 0.0)
+      throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
     for (int q = 0; q < m; q++) {
       al[q] = mir[2 * q];
       be[q] = mir[2 * q + 1];
@@ -453,6 +488,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     double *cd = cdev + (i & 1) * kMaxLanczosIterations;
     R *yi = yb + (size_t)(i & 1) * n;
     LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i & 1], 0));
+    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[4 * i + 2], sd));
     LMG_CUDA(cudaMemcpyAsync(cd, c, m * sizeof(double), cudaMemcpyHostToDevice, sd));
     krylov_estimate_kernel<R><<<blocks, kRedThreads, 0, sd>>>(V, n, m, cd, sc, yi, n);
     count_launch();
@@ -460,6 +496,10 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
       krylov_error_kernel<R><<<blocks, kRedThreads, 0, sd>>>(
           yi, yb + (size_t)((i + 1) & 1) * n, n, rp_side, tk_side, sc, mir_dev + 512);
       count_launch();
+    }
+    if (timing_) {
+      LMG_CUDA(cudaEventRecord(ev_phase_[4 * i + 3], sd));
+      checked.push_back(i);
     }
     LMG_CUDA(cudaEventRecord(ev_check_, sd));
     LMG_CUDA(cudaGetLastError());
@@ -488,6 +528,29 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
                            cudaMemcpyDeviceToDevice, sd));
   LMG_CUDA(cudaEventRecord(ev_side_, sd));
   LMG_CUDA(cudaStreamWaitEvent(st, ev_side_, 0));
+  if (timing_) {
+    // algorithmic bytes: per iteration w, v_i, v_{i-1} read and v_{i+1}
+    // written (4n); per check the m basis vectors read and y written, then
+    // y and the previous y read for the error (2n, from the second check on)
+    LMG_CUDA(cudaStreamSynchronize(st));
+    const double vb = (double)n * sizeof(R);
+    for (int j = 0; j < issued; j++) {
+      float ms = 0;
+      LMG_CUDA(cudaEventElapsedTime(&ms, ev_phase_[4 * j], ev_phase_[4 * j + 1]));
+      phase_.vector_ms += ms;
+      phase_.vector_bytes += 4 * vb;
+    }
+    for (size_t q = 0; q < checked.size(); q++) {
+      const int i = checked[q];
+      float ms = 0;
+      LMG_CUDA(cudaEventElapsedTime(&ms, ev_phase_[4 * i + 2], ev_phase_[4 * i + 3]));
+      phase_.check_ms += ms;
+      phase_.check_bytes += (i + 2) * vb + (q > 0 ? 2 * vb : 0);
+    }
+    phase_.iterations += issued;
+    phase_.checks += (long)checked.size();
+    phase_.solves += 1;
+  }
   return done;
 }
 

@@ -52,6 +52,20 @@ class SolverBase {
   // reference): kind "none" or "mlp" with the network's parameters
   virtual void set_preconditioner(const std::string &kind, const float *params, size_t n) = 0;
   int last_solve_iterations() const { return last_inner_iters_; }
+  // Lanczos phase timing (no counterpart in the reference), off by default:
+  // device time of the Krylov vector updates that follow each matvec (on the
+  // solver stream) and of the convergence checks (estimate y = |z| V c and
+  // the error norm, on the side stream, overlapping the next matvec), with
+  // the algorithmic bytes each moves, summed over converged solves.
+  struct PhaseTimes {
+    double vector_ms = 0, vector_bytes = 0, check_ms = 0, check_bytes = 0;
+    long iterations = 0, checks = 0, solves = 0;
+  };
+  void set_phase_timing(bool on) {
+    timing_ = on;
+    phase_ = PhaseTimes{};
+  }
+  const PhaseTimes &phase_times() const { return phase_; }
   // called at the end of initialize() with the seed as the caller gave it
   virtual void on_initialized(uint64_t user_seed) { (void)user_seed; }
 
@@ -89,6 +103,8 @@ class SolverBase {
   int hard_limit_ = 200;     // lanczos::Solver::iterationHardLimit
   lmg_lanczos_callback cb_ = nullptr;
   int last_inner_iters_ = 0;  // BiCGSTAB iterations of the last preconditioned solve
+  bool timing_ = false;
+  PhaseTimes phase_;
   void *cb_user_ = nullptr;
   // positions
   int64_t N_ = 0;

@@ -176,6 +176,21 @@ class NBody:
         self._check(self._lib.lmg_get_preconditioner_solve_iterations(self._h, ctypes.byref(it)))
         return it.value
 
+    def _lanczos_phase_timing(self, on=True):
+        """Measurement hook: time the Krylov vector updates and the convergence
+        checks of every following sqrtMdotW on the device (resets the sums)."""
+        self._check(self._lib.lmg_internal_lanczos_phase_timing(self._h, int(bool(on))))
+
+    def _lanczos_phase_times(self):
+        """Sums since the timing was switched on: milliseconds and algorithmic
+        bytes of the vector updates and of the checks, iterations issued
+        (including the one issued ahead of the last check), checks, solves."""
+        out = (ctypes.c_double * 7)()
+        self._check(self._lib.lmg_internal_lanczos_phase_times(self._h, out))
+        keys = ("vector_ms", "vector_bytes", "check_ms", "check_bytes", "iterations",
+                "checks", "solves")
+        return dict(zip(keys, list(out)))
+
     def setLanczosIterationLimit(self, limit):
         """lanczos::Solver::setIterationHardLimit (LanczosAlgorithm.h:272-274)."""
         self._check(self._lib.lmg_set_lanczos_iteration_limit(self._h, int(limit)))

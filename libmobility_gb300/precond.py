@@ -164,7 +164,7 @@ def _make_chunk(args):
     rng = np.random.default_rng(seed)
     Xs, Ys = [], []
     for _ in range(nsys):
-        n = int(rng.integers(64, 513))
+        n = int(rng.integers(max(64, k + 1), 513))  # every particle has k neighbours
         phi = float(rng.uniform(0.05, 0.3))
         p = random_system(rng, n, phi, rng.random() < 0.5)
         ids = rng.choice(n, min(n, per_sys), replace=False)

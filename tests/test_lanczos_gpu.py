@@ -170,3 +170,53 @@ def test_adaptive_check_schedule_matches_reference(cuda, oracle):
         _, _, it, _ = s.sqrtMdotW_noise(zz)
         _, ito = ref.run(lambda v: M @ v, zz, 1e-6)
         assert it == ito
+
+
+def test_phase_timing_counts_and_leaves_results_unchanged(cuda):
+    """The measurement hook only records events: two solvers with the same
+    history, one timed, give bitwise the same results; the sums count every
+    issued iteration (the one issued ahead of the last check included) and
+    the algorithmic bytes 4 n s per iteration."""
+    rng = np.random.default_rng(12)
+    N = 300
+    p = np.column_stack([rng.uniform(0, 40, (N, 2)), rng.uniform(1.5, 10, N)])
+    dWs = [rng.normal(size=6 * N) for _ in range(4)]
+    out = []
+    for timed in (False, True):
+        s = make_solver(1, 1, 1.0, 1.0, "float")
+        s.initialize(viscosity=1.0, hydrodynamicRadius=1.0, includeAngular=True,
+                     tolerance=1e-6)
+        s.setPositions(p)
+        if timed:
+            s._lanczos_phase_timing(True)
+        out.append([s.sqrtMdotW_noise(z) for z in dWs])
+    t = s._lanczos_phase_times()
+    its = 0
+    for a, b in zip(*out):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
+        its += b[2]
+    assert t["solves"] == 4 and t["checks"] >= 4
+    assert its <= t["iterations"] <= its + 2 * 4
+    assert t["vector_bytes"] == 4 * (6 * N) * 4 * t["iterations"]
+    assert t["check_bytes"] > 0 and t["vector_ms"] > 0 and t["check_ms"] > 0
+    s._lanczos_phase_timing(False)
+    assert s._lanczos_phase_times()["solves"] == 0  # switching resets the sums
+
+
+def test_grid_barrier_wait_is_bounded(cuda):
+    """The fused Lanczos step waits at grid barriers; a wait that nothing
+    ends gives up after about a second, reports, and leaves the context
+    usable (two blocks meeting at a barrier that cannot complete)."""
+    import ctypes
+    import time
+    from libmobility_gb300 import _capi
+    lib = _capi.load()
+    gave_up = ctypes.c_int()
+    t0 = time.perf_counter()
+    assert lib.lmg_internal_barrier_timeout_probe(ctypes.byref(gave_up)) == 0
+    assert gave_up.value == 2
+    assert time.perf_counter() - t0 < 30
+    s = make_solver(0, 0, 1.0, 1.0, "float")
+    s.setPositions(np.random.default_rng(2).uniform(0, 10, (30, 3)))
+    u, _ = s.sqrtMdotW()
+    assert np.isfinite(u).all() and np.abs(u).max() > 0
