@@ -30,7 +30,7 @@
 namespace lmg {
 
 // Network shape for K neighbours (16, 32, 48 or 64) and hidden width H (64, 128,
-// 256 or 512): parameters and normalisation, FP32, in one contiguous array:
+// 256, 512 or 1024): parameters and normalisation, FP32, in one contiguous array:
 //   W1[3K][H] b1[H] W2[H][H] b2[H] W3[H][6+9K] b3[6+9K]
 //   xmean[3K] xstd[3K] ymean[6+9K] ystd[6+9K]
 // Every (K, H) pair has a different parameter count, which identifies it.
@@ -63,7 +63,7 @@ inline PrecLayout prec_layout(int K, int H) {
 // The layout whose parameter count is n (K = 0 if there is none).
 inline PrecLayout prec_layout_for_params(size_t n) {
   for (int K : {16, 32, 48, 64})
-    for (int H : {64, 128, 256, 512}) {
+    for (int H : {64, 128, 256, 512, 1024}) {
       const PrecLayout L = prec_layout(K, H);
       if ((size_t)L.Params == n) return L;
     }

@@ -2,7 +2,7 @@
 csrc/precond.cuh for what P is and why it is sparse).
 
 Training data are made by the method itself: random small particle systems
-(N uniform in 64..512, volume fraction uniform in 0.05..0.3, half of them as
+(N uniform in max(64, K+1)..512, volume fraction uniform in 0.05..0.3, half of them as
 Gaussian clusters of ~128 particles with sigma = 4a, overlaps at 2a removed);
 for sampled particles the (K+1)-particle neighbourhood mobility (open-boundary
 RPY, t0 = 1, a = 1; K = 16, 32, 48 or 64 nearest neighbours) is inverted-square-
@@ -217,11 +217,11 @@ def ntrain(k, h=NH):
 def shape_of_params(n):
     """(k, h) of a flat parameter vector of length n."""
     for k in (16, 32, 48, 64):
-        for h in (64, 128, 256, 512):
+        for h in (64, 128, 256, 512, 1024):
             if n == sum(int(np.prod(s)) for _, s in layout(k, h)):
                 return k, h
     raise ValueError(f"{n} is not the parameter count of a K = 16, 32, 48 or 64 network "
-                     "with 64, 128, 256 or 512 hidden units")
+                     "with 64, 128, 256, 512 or 1024 hidden units")
 
 
 LAYOUT = layout(16)
@@ -398,7 +398,7 @@ def main():
     sub = ap.add_subparsers(dest="cmd")
     t = sub.add_parser("train")
     t.add_argument("--k", type=int, default=16, choices=[16, 32, 48, 64])
-    t.add_argument("--hidden", type=int, default=NH, choices=[64, 128, 256, 512])
+    t.add_argument("--hidden", type=int, default=NH, choices=[64, 128, 256, 512, 1024])
     t.add_argument("--systems", type=int, default=20000)
     t.add_argument("--per-system", type=int, default=32)
     t.add_argument("--epochs", type=int, default=60)

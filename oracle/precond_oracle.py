@@ -27,7 +27,7 @@ NIN, NOUT = 3 * K, 6 + 9 * K
 def kh_of(flat):
     """(neighbours, hidden units) of a flat parameter vector."""
     for k in (16, 32, 48, 64):
-        for h in (64, 128, 256, 512):
+        for h in (64, 128, 256, 512, 1024):
             if len(flat) == sum(int(np.prod(s)) for _, s in shapes(k, h)):
                 return k, h
     raise ValueError("not a preconditioner parameter vector")

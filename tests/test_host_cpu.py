@@ -37,7 +37,7 @@ def test_network_layouts_are_distinct_and_match_the_oracle():
     from oracle import precond_oracle as po
     seen = {}
     for k in (16, 32, 48, 64):
-        for h in (64, 128, 256, 512):
+        for h in (64, 128, 256, 512, 1024):
             n = sum(int(np.prod(s)) for _, s in precond.layout(k, h))
             assert n not in seen, (k, h, seen.get(n))
             seen[n] = (k, h)
