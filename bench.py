@@ -266,7 +266,8 @@ def sqrtmdotw_comparison(torch, steps, warmup, rank, N=65536):
                 inner.append(s.lastPreconditionerSolveIterations() if kind == "mlp" else 0)
         t = sum(times) / len(times)
         out[kind] = {"solves_per_s": 1.0 / t, "ms_per_solve": t * 1e3,
-                     "lanczos_iterations": sum(its) / len(its)}
+                     "lanczos_iterations": sum(its) / len(its),
+                     "iterations_min_max": [min(its), max(its)], "solves": len(its)}
         if kind == "mlp":
             out[kind]["p_solve_iterations"] = sum(inner) / len(inner)
     out["speedup_learned_vs_plain"] = out["mlp"]["solves_per_s"] / out["none"]["solves_per_s"]
@@ -614,7 +615,9 @@ def run_ours(args, w, ws, rank, local):
 
     cmp = None
     if not args.skip_precond:
-        cmp = sqrtmdotw_comparison(torch, max(2, args.steps), 2, rank)
+        # the preconditioned stopping step moves by +-4 from one dW to the next:
+        # at least 8 solves per arm
+        cmp = sqrtmdotw_comparison(torch, max(8, args.steps), 2, rank)
     ens = None
     if not args.skip_ensemble:
         ens = ensemble_comparison(torch, max(2, args.steps), 2, rank)

@@ -471,7 +471,7 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
 constexpr int kRowX = 64, kRowSplit = 4;
 
 template <int KB, class T>
-__global__ void __launch_bounds__(kRowX * kRowSplit)
+__global__ void __launch_bounds__(kRowX * kRowSplit, 8)
 precond_apply_kernel(const T *__restrict__ B, const int *__restrict__ nb, int N,
                      const float *__restrict__ x, float *__restrict__ out, float scale) {
   __shared__ float part[kRowSplit][3][kRowX];
@@ -480,7 +480,7 @@ precond_apply_kernel(const T *__restrict__ B, const int *__restrict__ nb, int N,
   const size_t sN = (size_t)N;
   float o0 = 0.f, o1 = 0.f, o2 = 0.f;
   if (i < N) {
-#pragma unroll 4
+#pragma unroll 2
     for (int n = q; n < KB; n += kRowSplit) {
       const int j = nb[n * sN + i];
       const T *b = B + (size_t)n * 9 * sN + i;  // b[e * N]: element e of block n
@@ -502,32 +502,44 @@ precond_apply_kernel(const T *__restrict__ B, const int *__restrict__ nb, int N,
   }
 }
 
-// P^T x: one thread per row scatters with atomics (splitting the row over
-// more threads, as in the product above, made the atomics slower)
+// P^T x: one thread per row scatters its K+1 products with one 16-byte
+// vector atomic each into a float4-padded copy of the output (a third of
+// the L2 atomic operations of three scalar ones, which saturated L2), then
+// a second pass packs the padded copy into the 3-component output.
 template <int KB, class T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 precond_apply_t_kernel(const T *__restrict__ B, const int *__restrict__ nb, int N,
-                       const float *__restrict__ x, float *out, float scale) {
+                       const float *__restrict__ x, float4 *pad, float scale) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const size_t sN = (size_t)N;
   const float v0 = scale * x[3 * i], v1 = scale * x[3 * i + 1], v2 = scale * x[3 * i + 2];
-#pragma unroll 7
+#pragma unroll 4
   for (int n = 0; n < KB; n++) {
     const int j = nb[n * sN + i];
     const T *b = B + (size_t)n * 9 * sN + i;
-    atomicAdd(out + 3 * j, ldf(b) * v0 + ldf(b + 3 * sN) * v1 + ldf(b + 6 * sN) * v2);
-    atomicAdd(out + 3 * j + 1, ldf(b + sN) * v0 + ldf(b + 4 * sN) * v1 + ldf(b + 7 * sN) * v2);
-    atomicAdd(out + 3 * j + 2,
-              ldf(b + 2 * sN) * v0 + ldf(b + 5 * sN) * v1 + ldf(b + 8 * sN) * v2);
+    atomicAdd(pad + j,
+              make_float4(ldf(b) * v0 + ldf(b + 3 * sN) * v1 + ldf(b + 6 * sN) * v2,
+                          ldf(b + sN) * v0 + ldf(b + 4 * sN) * v1 + ldf(b + 7 * sN) * v2,
+                          ldf(b + 2 * sN) * v0 + ldf(b + 5 * sN) * v1 + ldf(b + 8 * sN) * v2,
+                          0.f));
   }
+}
+
+__global__ void __launch_bounds__(256) unpad3_kernel(const float4 *pad, int N, float *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const float4 p = pad[i];
+  out[3 * i] = p.x;
+  out[3 * i + 1] = p.y;
+  out[3 * i + 2] = p.z;
 }
 
 template <int KB, class T>
 void apply_dispatch(bool transpose, const T *B, const int *nb, int N, const float *x, float *out,
-                    float scale, cudaStream_t stream) {
+                    float4 *pad, float scale, cudaStream_t stream) {
   if (transpose)
-    precond_apply_t_kernel<KB, T><<<(N + 255) / 256, 256, 0, stream>>>(B, nb, N, x, out, scale);
+    precond_apply_t_kernel<KB, T><<<(N + 255) / 256, 256, 0, stream>>>(B, nb, N, x, pad, scale);
   else
     precond_apply_kernel<KB, T><<<(N + kRowX - 1) / kRowX, dim3(kRowX, kRowSplit), 0, stream>>>(
         B, nb, N, x, out, scale);
@@ -535,29 +547,39 @@ void apply_dispatch(bool transpose, const T *B, const int *nb, int N, const floa
 
 template <class T>
 cudaError_t apply_k(int K, bool transpose, const void *blocks, const int *nb, int N,
-                    const float *x, float *out, float scale, cudaStream_t stream) {
+                    const float *x, float *out, float4 *pad, float scale, cudaStream_t stream) {
   const T *B = static_cast<const T *>(blocks);
   if (K != 16 && K != 32 && K != 48 && K != 64) return cudaErrorInvalidValue;
+  if (N <= 0) return cudaSuccess;
+  if (transpose) {
+    if (!pad) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(pad, 0, (size_t)N * sizeof(float4), stream);
+    if (e != cudaSuccess) return e;
+  }
   count_launch();
-  if (K == 16) apply_dispatch<17, T>(transpose, B, nb, N, x, out, scale, stream);
-  if (K == 32) apply_dispatch<33, T>(transpose, B, nb, N, x, out, scale, stream);
-  if (K == 48) apply_dispatch<49, T>(transpose, B, nb, N, x, out, scale, stream);
-  if (K == 64) apply_dispatch<65, T>(transpose, B, nb, N, x, out, scale, stream);
+  if (K == 16) apply_dispatch<17, T>(transpose, B, nb, N, x, out, pad, scale, stream);
+  if (K == 32) apply_dispatch<33, T>(transpose, B, nb, N, x, out, pad, scale, stream);
+  if (K == 48) apply_dispatch<49, T>(transpose, B, nb, N, x, out, pad, scale, stream);
+  if (K == 64) apply_dispatch<65, T>(transpose, B, nb, N, x, out, pad, scale, stream);
+  if (transpose) {
+    count_launch();
+    unpad3_kernel<<<(N + 255) / 256, 256, 0, stream>>>(pad, N, out);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t precond_apply_launch(int K, const void *blocks, bool half, float scale,
                                  const int *nb, int N, const float *x, float *out,
                                  cudaStream_t stream) {
-  return half ? apply_k<__half>(K, false, blocks, nb, N, x, out, scale, stream)
-              : apply_k<float>(K, false, blocks, nb, N, x, out, scale, stream);
+  return half ? apply_k<__half>(K, false, blocks, nb, N, x, out, nullptr, scale, stream)
+              : apply_k<float>(K, false, blocks, nb, N, x, out, nullptr, scale, stream);
 }
 
 cudaError_t precond_apply_t_launch(int K, const void *blocks, bool half, float scale,
                                    const int *nb, int N, const float *x, float *out,
-                                   cudaStream_t stream) {
-  return half ? apply_k<__half>(K, true, blocks, nb, N, x, out, scale, stream)
-              : apply_k<float>(K, true, blocks, nb, N, x, out, scale, stream);
+                                   float4 *pad, cudaStream_t stream) {
+  return half ? apply_k<__half>(K, true, blocks, nb, N, x, out, pad, scale, stream)
+              : apply_k<float>(K, true, blocks, nb, N, x, out, pad, scale, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -820,14 +842,29 @@ int lmg_internal_precond_build_kh(int K, int H, const float *pos, const int *nb,
   }
 }
 
+
+// Either product with float (half = 0) or half blocks (half = 1, applied
+// with scale 1).  The transposed product needs a float4 work array of N
+// entries: `pad`, or one allocated and freed here (the call then waits).
+int lmg_internal_precond_apply_kh(int K, const void *blocks, int half, const int *nb, int N,
+                                  const float *x, float *out, int transpose, float *pad,
+                                  void *stream) {
+  const cudaStream_t st = (cudaStream_t)stream;
+  if (!transpose)
+    return (int)precond_apply_launch(K, blocks, half != 0, 1.0f, nb, N, x, out, st);
+  float4 *p = reinterpret_cast<float4 *>(pad);
+  if (p) return (int)precond_apply_t_launch(K, blocks, half != 0, 1.0f, nb, N, x, out, p, st);
+  cudaError_t e = cudaMalloc(&p, (size_t)std::max(N, 1) * sizeof(float4));
+  if (e != cudaSuccess) return (int)e;
+  e = precond_apply_t_launch(K, blocks, half != 0, 1.0f, nb, N, x, out, p, st);
+  const cudaError_t e2 = cudaStreamSynchronize(st);
+  cudaFree(p);
+  return (int)(e != cudaSuccess ? e : e2);
+}
+
 int lmg_internal_precond_apply_k(int K, const float *blocks, const int *nb, int N,
                                  const float *x, float *out, int transpose, void *stream) {
-  if (transpose) {
-    cudaMemsetAsync(out, 0, 3 * (size_t)N * sizeof(float), (cudaStream_t)stream);
-    return (int)precond_apply_t_launch(K, blocks, false, 1.0f, nb, N, x, out,
-                                       (cudaStream_t)stream);
-  }
-  return (int)precond_apply_launch(K, blocks, false, 1.0f, nb, N, x, out, (cudaStream_t)stream);
+  return lmg_internal_precond_apply_kh(K, blocks, 0, nb, N, x, out, transpose, nullptr, stream);
 }
 
 // K = 16 forms

@@ -106,9 +106,10 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
 cudaError_t precond_apply_launch(int K, const void *blocks, bool half, float scale,
                                  const int *nb, int N, const float *x, float *out,
                                  cudaStream_t stream);
-// out_{nb[n][i]} += scale B[n][i]^T x_i    (P^T x); out must be zeroed first
+// out_j = scale sum_{(n,i): nb[n][i] = j} B[n][i]^T x_i    (P^T x), through
+// the work array pad[N] (float4, 16-byte aligned), which it zeroes first
 cudaError_t precond_apply_t_launch(int K, const void *blocks, bool half, float scale,
                                    const int *nb, int N, const float *x, float *out,
-                                   cudaStream_t stream);
+                                   float4 *pad, cudaStream_t stream);
 
 }  // namespace lmg

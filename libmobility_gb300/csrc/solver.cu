@@ -154,6 +154,7 @@ template <class R> class Solver final : public SolverBase {
   DeviceBuffer<int> prec_nb_;
   KnnScratch knn_scratch_;
   DeviceBuffer<R> pt_, pu_, bx_, br_, brh_, bp_, bv_, bs_, bt_;  // operator and BiCGSTAB vectors
+  DeviceBuffer<float> ppad_;  // float4-padded work array of the P^T product
   int num_sms_ = 0;
   int step_per_sm_ = 0;  // resident krylov_step_kernel blocks per SM
   bool tickets_zeroed_ = false;
@@ -800,8 +801,9 @@ template <class R> void Solver<R>::apply_operator(const R *v, R *out) {
     R *t = pt_.ensure(n);
     R *u = pu_.ensure(n);
     const R s = (R)(1.0 / std::sqrt(r0_));  // angular part: scalar r0^{-1/2}
-    LMG_CUDA(cudaMemsetAsync(t, 0, n3 * sizeof(R), stream()));
-    LMG_CUDA(precond_apply_t_launch(prec_k_, prec_blocks_.ptr, true, prec_scale(), prec_nb_.ptr, N, v, t, stream()));
+    float4 *pad = reinterpret_cast<float4 *>(ppad_.ensure(4 * (size_t)N));
+    LMG_CUDA(precond_apply_t_launch(prec_k_, prec_blocks_.ptr, true, prec_scale(), prec_nb_.ptr, N,
+                                    v, t, pad, stream()));
     if (ang_) {
       scale_kernel<R><<<vec_blocks(n3), kRedThreads, 0, stream()>>>(t + n3, v + n3, n3, s);
       count_launch();

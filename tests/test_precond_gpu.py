@@ -155,6 +155,38 @@ def test_wider_networks_match_oracle(cuda, po, K, H):
         assert np.allclose(out.cpu().numpy(), ref_y, rtol=1e-4, atol=1e-5 * np.abs(ref_y).max())
 
 
+@pytest.mark.parametrize("K", [16, 48, 64])
+def test_half_block_products_match_dense(cuda, po, K):
+    """P x and P^T x with half-precision blocks (the solver's storage), the
+    transposed one through the float4 work array given or allocated, against
+    the dense P of the same half-rounded blocks."""
+    import torch
+    lib = _lib()
+    rng = np.random.default_rng(K)
+    N = 3 * K + 50
+    p = _clustered(rng, N).astype(np.float32)
+    dp = torch.tensor(p, device="cuda")
+    nb = torch.empty((K + 1, N), dtype=torch.int32, device="cuda")
+    assert lib.lmg_internal_knn_k(K, ctypes.c_void_p(dp.data_ptr()), N, N,
+                                  ctypes.c_void_p(nb.data_ptr()), None) == 0
+    blocks = torch.tensor(rng.normal(0, 0.3, (K + 1, 9, N)), dtype=torch.float16, device="cuda")
+    got = blocks.float().cpu().numpy().transpose(2, 0, 1).reshape(N, K + 1, 3, 3)
+    P = po.dense_p(got.astype(np.float64), nb.cpu().numpy().T)
+    x = rng.normal(size=3 * N).astype(np.float32)
+    dx = torch.tensor(x, device="cuda")
+    pad = torch.full((4 * N,), 7.0, device="cuda")  # the product zeroes it first
+    for tr, ref_y in ((0, P @ x), (1, P.T @ x)):
+        for work in (pad, None):
+            out = torch.full((3 * N,), 5.0, device="cuda")  # overwritten
+            assert lib.lmg_internal_precond_apply_kh(
+                K, ctypes.c_void_p(blocks.data_ptr()), 1, ctypes.c_void_p(nb.data_ptr()), N,
+                ctypes.c_void_p(dx.data_ptr()), ctypes.c_void_p(out.data_ptr()), tr,
+                None if work is None else ctypes.c_void_p(work.data_ptr()), None) == 0
+            torch.cuda.synchronize()
+            assert np.allclose(out.cpu().numpy(), ref_y, rtol=1e-4,
+                               atol=1e-5 * np.abs(ref_y).max()), (tr, work is None)
+
+
 @pytest.mark.parametrize("ta,tb", [(0, 0), (1, 0), (0, 1), (1, 1)])
 def test_large_gemm_matches_numpy(cuda, ta, tb):
     """The register-blocked GEMM (used from 64 output tiles of 128 x 128 on):
