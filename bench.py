@@ -674,7 +674,7 @@ def main():
                     help="skip the batched ensemble of 256 uneven systems")
     ap.add_argument("--skip-large", action="store_true",
                     help="skip the N = 262144 single-wall Mdot")
-    ap.add_argument("--only", choices=["ensemble"], default=None,
+    ap.add_argument("--only", choices=["ensemble", "precond"], default=None,
                     help="run one sub-measurement alone and print it (for profiling)")
     ap.add_argument("--ensemble-systems", type=int, default=256)
     args = ap.parse_args()
@@ -686,6 +686,12 @@ def main():
                                   sequential=False)
         if rank == 0:
             print(json.dumps({"ensemble": out}))
+        return
+    if args.only == "precond":  # plain vs learned sqrtMdotW alone (profiling runs)
+        import torch
+        out = sqrtmdotw_comparison(torch, args.steps, args.warmup, rank)
+        if rank == 0:
+            print(json.dumps({"sqrtMdotW_learned_vs_plain": out}))
         return
     if args.impl == "reference":
         run_reference(args, w, ws, rank)
