@@ -270,6 +270,20 @@ def sqrtmdotw_comparison(torch, steps, warmup, rank, N=65536):
                      "iterations_min_max": [min(its), max(its)], "solves": len(its)}
         if kind == "mlp":
             out[kind]["p_solve_iterations"] = sum(inner) / len(inner)
+        # where the time goes: device spans of two more solves, outside the
+        # timed ones (the events add a synchronisation at the end of a solve)
+        s._lanczos_phase_timing(True)
+        for dW in dWs[warmup:warmup + 2]:
+            s.setPositions(dpos)
+            s.sqrtMdotW_noise(dW)
+        torch.cuda.synchronize()
+        ph = s._lanczos_phase_times()
+        s._lanczos_phase_timing(False)
+        nit = ph["iterations"]
+        out[kind]["per_iteration_us"] = {
+            "operator": 1e3 * ph["operator_ms"] / nit, "vector_update": 1e3 * ph["vector_ms"] / nit}
+        out[kind]["per_solve_ms"] = {"preconditioner_build": ph["build_ms"] / ph["solves"],
+                                     "p_solve": ph["psolve_ms"] / ph["solves"]}
     out["speedup_learned_vs_plain"] = out["mlp"]["solves_per_s"] / out["none"]["solves_per_s"]
     return out
 

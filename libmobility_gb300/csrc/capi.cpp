@@ -218,8 +218,8 @@ int lmg_internal_tridiag_sqrt_e1(const double *alpha, const double *beta, int m,
 
 // Internal measurement hooks (not part of the public header): switch the
 // Lanczos phase timing on or off (either resets the sums), and read the sums
-// as out[7] = {vector_ms, vector_bytes, check_ms, check_bytes, iterations,
-// checks, solves}.
+// as out[10] = {vector_ms, vector_bytes, check_ms, check_bytes, iterations,
+// checks, solves, operator_ms, build_ms, psolve_ms}.
 int lmg_internal_lanczos_phase_timing(lmg_solver *h, int on) {
   return guarded(h, [&](lmg::SolverBase &m) { m.set_phase_timing(on != 0); });
 }
@@ -227,9 +227,11 @@ int lmg_internal_lanczos_phase_timing(lmg_solver *h, int on) {
 int lmg_internal_lanczos_phase_times(lmg_solver *h, double *out) {
   if (!h || !h->impl || !out) return LMG_ERR_INVALID_ARGUMENT;
   const auto &p = h->impl->phase_times();
-  const double v[7] = {p.vector_ms, p.vector_bytes, p.check_ms, p.check_bytes,
-                       (double)p.iterations, (double)p.checks, (double)p.solves};
-  for (int q = 0; q < 7; q++) out[q] = v[q];
+  const double v[10] = {p.vector_ms,         p.vector_bytes,   p.check_ms,
+                        p.check_bytes,       (double)p.iterations, (double)p.checks,
+                        (double)p.solves,    p.operator_ms,    p.build_ms,
+                        p.psolve_ms};
+  for (int q = 0; q < 10; q++) out[q] = v[q];
   return LMG_OK;
 }
 

@@ -100,6 +100,8 @@ template <class R> class Solver final : public SolverBase {
     if (ev_side_) cudaEventDestroy(ev_side_);
     for (auto &e : ev_phase_)
       if (e) cudaEventDestroy(e);
+    for (auto &e : ev_pre_)
+      if (e) cudaEventDestroy(e);
     if (side_) cudaStreamDestroy(side_);
   }
 
@@ -136,9 +138,12 @@ template <class R> class Solver final : public SolverBase {
   PinnedBuffer<double> h_dbl_;
   cudaStream_t side_ = nullptr;       // high-priority stream for per-check work
   cudaEvent_t ev_iter_[2] = {nullptr, nullptr}, ev_check_ = nullptr, ev_side_ = nullptr;
-  // phase timing: per iteration j, [4j, 4j+1] bracket the vector updates and
-  // [4j+2, 4j+3] the check (created on the first timed solve)
+  // phase timing: per iteration j, [5j, 5j+1] bracket the operator, [5j+1,
+  // 5j+2] the vector updates and [5j+3, 5j+4] the check; ev_pre_ the
+  // preconditioner build and P solve (created on the first timed solve)
   std::vector<cudaEvent_t> ev_phase_;
+  cudaEvent_t ev_pre_[4] = {nullptr, nullptr, nullptr, nullptr};
+  void ensure_phase_events();
   // RFD
   DeviceBuffer<R> rfd_noise_, rfd_pos_, rfd_mp_, rfd_mm_;
   // learned preconditioner
@@ -393,6 +398,15 @@ template <class R> void Solver<R>::ensure_side() {
 // y_i = |z| V c_i and |y_i - y_{i-1}| / |y_{i-1}|, and reads the error back.
 // At the first check of a solve there is no y_{i-1}; its error counts as
 // infinite (the reference compares against a zero or stale buffer there).
+template <class R> void Solver<R>::ensure_phase_events() {
+  if (ev_phase_.empty()) {
+    ev_phase_.assign(5 * (kMaxLanczosIterations + 1), nullptr);
+    for (auto &e : ev_phase_) LMG_CUDA(cudaEventCreate(&e));
+  }
+  for (auto &e : ev_pre_)
+    if (!e) LMG_CUDA(cudaEventCreate(&e));
+}
+
 template <class R>
 int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *residual) {
   const int limit = hard_limit_;
@@ -440,16 +454,14 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
   krylov_scale_first_kernel<R><<<blocks, kRedThreads, 0, st>>>(z, V, n, sc);
   count_launch();
 
-  if (timing_ && ev_phase_.empty()) {
-    ev_phase_.assign(4 * (kMaxLanczosIterations + 1), nullptr);
-    for (auto &e : ev_phase_) LMG_CUDA(cudaEventCreate(&e));
-  }
+  if (timing_) ensure_phase_events();
   int issued = 0;
   std::vector<int> checked;
   auto issue = [&](int j) {
     R *vj = V + (size_t)j * n;
+    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * j], st));
     apply_operator(vj, w);
-    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[4 * j], st));
+    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * j + 1], st));
     const R *vprev = j > 0 ? vj - n : vj;
     R *vnext = vj + n;
     size_t nn = n;
@@ -459,7 +471,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     LMG_CUDA(cudaLaunchCooperativeKernel((const void *)krylov_step_kernel<R>, dim3(step_blocks),
                                          dim3(kRedThreads), args, 0, st));
     count_launch();
-    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[4 * j + 1], st));
+    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * j + 2], st));
     LMG_CUDA(cudaEventRecord(ev_iter_[j & 1], st));
     issued = j + 1;
   };
@@ -489,7 +501,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     double *cd = cdev + (i & 1) * kMaxLanczosIterations;
     R *yi = yb + (size_t)(i & 1) * n;
     LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i & 1], 0));
-    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[4 * i + 2], sd));
+    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
     LMG_CUDA(cudaMemcpyAsync(cd, c, m * sizeof(double), cudaMemcpyHostToDevice, sd));
     krylov_estimate_kernel<R><<<blocks, kRedThreads, 0, sd>>>(V, n, m, cd, sc, yi, n);
     count_launch();
@@ -499,7 +511,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
       count_launch();
     }
     if (timing_) {
-      LMG_CUDA(cudaEventRecord(ev_phase_[4 * i + 3], sd));
+      LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 4], sd));
       checked.push_back(i);
     }
     LMG_CUDA(cudaEventRecord(ev_check_, sd));
@@ -536,15 +548,17 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     LMG_CUDA(cudaStreamSynchronize(st));
     const double vb = (double)n * sizeof(R);
     for (int j = 0; j < issued; j++) {
-      float ms = 0;
-      LMG_CUDA(cudaEventElapsedTime(&ms, ev_phase_[4 * j], ev_phase_[4 * j + 1]));
+      float op = 0, ms = 0;
+      LMG_CUDA(cudaEventElapsedTime(&op, ev_phase_[5 * j], ev_phase_[5 * j + 1]));
+      LMG_CUDA(cudaEventElapsedTime(&ms, ev_phase_[5 * j + 1], ev_phase_[5 * j + 2]));
+      phase_.operator_ms += op;
       phase_.vector_ms += ms;
       phase_.vector_bytes += 4 * vb;
     }
     for (size_t q = 0; q < checked.size(); q++) {
       const int i = checked[q];
       float ms = 0;
-      LMG_CUDA(cudaEventElapsedTime(&ms, ev_phase_[4 * i + 2], ev_phase_[4 * i + 3]));
+      LMG_CUDA(cudaEventElapsedTime(&ms, ev_phase_[5 * i + 3], ev_phase_[5 * i + 4]));
       phase_.check_ms += ms;
       phase_.check_bytes += (i + 2) * vb + (q > 0 ? 2 * vb : 0);
     }
@@ -606,13 +620,29 @@ void Solver<R>::sqrt_mdot_w(void *U, size_t nU, void *W, size_t nW, double prefa
   R *y = y_.ensure(n);
   double res = 0;
   const bool prec = prec_active();
+  const bool tp = timing_ && prec;
+  if (tp) {
+    ensure_phase_events();
+    LMG_CUDA(cudaEventRecord(ev_pre_[0], stream()));
+  }
   if (prec) prec_build();
+  if (tp) LMG_CUDA(cudaEventRecord(ev_pre_[1], stream()));
   const int it = lanczos(z, y, n, tol_, &res);
   if (prec) {
     // y currently holds S^{1/2} z with S = P M P^T; the sample is P^{-1} of it
     // (translational part by BiCGSTAB, angular part by the scalar factor)
     R *x = bx_.ensure(n);
+    if (tp) LMG_CUDA(cudaEventRecord(ev_pre_[2], stream()));
     last_inner_iters_ = solve_p(y, x);
+    if (tp) {
+      LMG_CUDA(cudaEventRecord(ev_pre_[3], stream()));
+      LMG_CUDA(cudaEventSynchronize(ev_pre_[3]));
+      float b = 0, q = 0;
+      LMG_CUDA(cudaEventElapsedTime(&b, ev_pre_[0], ev_pre_[1]));
+      LMG_CUDA(cudaEventElapsedTime(&q, ev_pre_[2], ev_pre_[3]));
+      phase_.build_ms += b;
+      phase_.psolve_ms += q;
+    }
     if (ang_) {
       const R sc = (R)std::sqrt(r0_);
       scale_kernel<R><<<vec_blocks(n3), kRedThreads, 0, stream()>>>(x + n3, y + n3, n3, sc);

@@ -60,6 +60,10 @@ class SolverBase {
   struct PhaseTimes {
     double vector_ms = 0, vector_bytes = 0, check_ms = 0, check_bytes = 0;
     long iterations = 0, checks = 0, solves = 0;
+    // the operator of each iteration (M v, or P M P^T v), and with the
+    // learned preconditioner its build and the final P solve (spans on the
+    // solver stream, idle gaps included)
+    double operator_ms = 0, build_ms = 0, psolve_ms = 0;
   };
   void set_phase_timing(bool on) {
     timing_ = on;

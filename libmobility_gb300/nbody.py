@@ -184,11 +184,13 @@ class NBody:
     def _lanczos_phase_times(self):
         """Sums since the timing was switched on: milliseconds and algorithmic
         bytes of the vector updates and of the checks, iterations issued
-        (including the one issued ahead of the last check), checks, solves."""
-        out = (ctypes.c_double * 7)()
+        (including the one issued ahead of the last check), checks, solves,
+        milliseconds of the operator (all iterations) and, with the learned
+        preconditioner, of its build and of the final P solve."""
+        out = (ctypes.c_double * 10)()
         self._check(self._lib.lmg_internal_lanczos_phase_times(self._h, out))
         keys = ("vector_ms", "vector_bytes", "check_ms", "check_bytes", "iterations",
-                "checks", "solves")
+                "checks", "solves", "operator_ms", "build_ms", "psolve_ms")
         return dict(zip(keys, list(out)))
 
     def setLanczosIterationLimit(self, limit):

@@ -199,6 +199,7 @@ def test_phase_timing_counts_and_leaves_results_unchanged(cuda):
     assert its <= t["iterations"] <= its + 2 * 4
     assert t["vector_bytes"] == 4 * (6 * N) * 4 * t["iterations"]
     assert t["check_bytes"] > 0 and t["vector_ms"] > 0 and t["check_ms"] > 0
+    assert t["operator_ms"] > 0 and t["build_ms"] == 0 and t["psolve_ms"] == 0
     s._lanczos_phase_timing(False)
     assert s._lanczos_phase_times()["solves"] == 0  # switching resets the sums
 
