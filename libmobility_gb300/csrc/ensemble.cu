@@ -54,6 +54,7 @@ namespace {
 constexpr int kPad = 128;            // systems padded to a multiple of this
 constexpr int kEnsThreads = 256;     // threads of the per-system vector kernels
 constexpr int kEnsLimit = 200;       // lanczos::Solver::iterationHardLimit
+constexpr int kEstChunk = 4 * kEnsThreads;  // elements of one system per estimate CTA
 constexpr double kDummyFar = 1e5;    // dummy particles: radii away from everything
 
 bool ens_is_device_ptr(const void *p) {
@@ -220,20 +221,29 @@ __global__ void ens_iter_inc(int *iter) { *iter += 1; }
 
 // Result estimate y_s = |z_s| V_s c_s (m basis vectors) for the systems due
 // for a check, written to ynew, and err_s = |y_s - yold_s| / |yold_s|
-// (LanczosAlgorithm.cu:202-222).
+// (LanczosAlgorithm.cu:202-222).  CTA (s, c) takes elements [c, c+1) x
+// kEstChunk of system s (one CTA per system left a 4000-particle system's
+// estimate to a single SM, slower than an iteration's products); the last
+// CTA of a system to finish sums the chunks' partial norms in chunk order.
 template <class R>
 __global__ void ens_estimate(const R *V, size_t ldv, int m, const double *coef, int lim,
                              const int *due, const double *normz, const int *off3,
-                             const int *nn, R *ynew, const R *yold, double *err) {
+                             const int *nn, R *ynew, const R *yold, double *part,
+                             unsigned *ticket, double *err) {
   const int s = blockIdx.x;
   if (!due[s]) return;
+  const int n = nn[s];
+  const int nch = (n + kEstChunk - 1) / kEstChunk, c = blockIdx.y;
+  if (c >= nch) return;
   __shared__ R cs[kEnsLimit + 1];
+  __shared__ bool s_last;
   const double nz = normz[s];
   for (int k = threadIdx.x; k < m; k += kEnsThreads) cs[k] = (R)(nz * coef[s * lim + k]);
   __syncthreads();
-  const int o = off3[s], n = nn[s];
+  const int o = off3[s];
+  const int e_end = min(n, (c + 1) * kEstChunk);
   double v[2] = {0.0, 0.0};
-  for (int e = threadIdx.x; e < n; e += kEnsThreads) {
+  for (int e = c * kEstChunk + threadIdx.x; e < e_end; e += kEnsThreads) {
     // eight independent partial sums: eight basis-vector loads in flight
     R part[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const R *col = V + o + e;
@@ -251,7 +261,25 @@ __global__ void ens_estimate(const R *V, size_t ldv, int m, const double *coef, 
     v[1] += d * d;
   }
   block_sum<2>(v);
-  if (threadIdx.x == 0) err[s] = fabs(sqrt(v[1]) / sqrt(v[0]));
+  double *mine = part + ((size_t)s * gridDim.y + c) * 2;
+  if (threadIdx.x == 0) {
+    __stcg(mine, v[0]);
+    __stcg(mine + 1, v[1]);
+    __threadfence();
+    s_last = atomicAdd(ticket + s, 1u) == (unsigned)(nch - 1);
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    const double *ps = part + (size_t)s * gridDim.y * 2;
+    double a = 0.0, d = 0.0;
+    for (int q = 0; q < nch; q++) {
+      a += __ldcg(ps + 2 * q);
+      d += __ldcg(ps + 2 * q + 1);
+    }
+    err[s] = fabs(sqrt(d) / sqrt(a));
+    ticket[s] = 0u;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -480,6 +508,11 @@ template <class R> class Ensemble final : public EnsembleBase {
   DeviceBuffer<double> sheight_, normz_, alpha_, beta_;
   DeviceBuffer<R> pos_, in_, out_, ustage_, ustage2_, V_, w_, vcur_, z_, yb_, part_;
   DeviceBuffer<unsigned> tickets_;
+  // estimate partial norms [system][chunk][2] and per-system tickets
+  // (self-resetting, zeroed when allocated)
+  int est_chunks_ = 1;
+  DeviceBuffer<double> est_part_;
+  DeviceBuffer<unsigned> est_ticket_;
   PinnedBuffer<R> pin_;
   PinnedBuffer<int> hflags_;
   MappedBuffer<double> hab_, coef_, err_;
@@ -584,6 +617,14 @@ void Ensemble<R>::set_systems(int nsys, const int *sizes, const int *geometry,
     sh[q] = height_u_[s];
     off3[q] = 3 * ioff_[q];
     nn[q] = 3 * sizes[s];
+  }
+  int maxn = 1;
+  for (int q = 0; q < nsys; q++) maxn = std::max(maxn, nn[q]);
+  est_chunks_ = (maxn + kEstChunk - 1) / kEstChunk;
+  est_part_.ensure((size_t)nsys * est_chunks_ * 2);
+  if (est_ticket_.count < (size_t)nsys) {
+    est_ticket_.ensure(nsys);
+    LMG_CUDA(cudaMemset(est_ticket_.ptr, 0, est_ticket_.count * sizeof(unsigned)));
   }
   auto up = [](DeviceBuffer<int> &b, const std::vector<int> &v) {
     int *d = b.ensure(v.size());
@@ -896,11 +937,10 @@ void Ensemble<R>::sqrt_mdot_w(const void *dW, size_t ndW, void *U, size_t nU, do
     });
     for (int q : due_list) due[q] = 1;
     LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i & 1], 0));
-    ens_estimate<R><<<nsys_, kEnsThreads, 0, sd>>>(V, ld, m, coef_.device_ptr(), lim,
-                                                   due_.device_ptr(), nz, off3_.ptr, nn_.ptr,
-                                                   yb + (size_t)(i & 1) * ld,
-                                                   yb + (size_t)((i + 1) & 1) * ld,
-                                                   err_.device_ptr());
+    ens_estimate<R><<<dim3(nsys_, est_chunks_), kEnsThreads, 0, sd>>>(
+        V, ld, m, coef_.device_ptr(), lim, due_.device_ptr(), nz, off3_.ptr, nn_.ptr,
+        yb + (size_t)(i & 1) * ld, yb + (size_t)((i + 1) & 1) * ld, est_part_.ptr,
+        est_ticket_.ptr, err_.device_ptr());
     count_launch();
     LMG_CUDA(cudaGetLastError());
     LMG_CUDA(cudaEventRecord(ev_check_, sd));
