@@ -166,52 +166,105 @@ __global__ void ens_first(const R *z, R *V0, R *vcur, const int *off3, const int
   }
 }
 
-// One Lanczos iteration i = *iter for every active system (one CTA each),
-// after w = M v_i:  w -= beta_{i-1} v_{i-1};  alpha_i = w.v_i;
-// w -= alpha_i v_i;  beta_i = |w| (0 below 1e-3 alpha_i/|z|);
-// v_{i+1} = w/beta_i or e1 (KrylovSubspace, LanczosAlgorithm.cu:131-152).
-// alpha_i, beta_i go to device arrays and to mapped host memory.
+// One Lanczos iteration i = *iter for every active system, after w = M v_i
+// (KrylovSubspace, LanczosAlgorithm.cu:131-152), split over CTAs (s, c), c a
+// chunk of kEstChunk elements of system s, in three launches (one CTA per
+// system took a fifth of an iteration for the largest systems).  Each
+// reduction goes through per-system chunk partials, summed in chunk order by
+// the last CTA of the system to finish (ticket), which publishes the scalar.
 template <class R>
-__global__ void ens_step(R *w, R *V, R *vcur, size_t ldv, const int *iter, const int *off3,
-                         const int *nn, const int *active, const double *normz, double *alpha,
-                         double *beta, int lim, double *host_ab) {
+__device__ __forceinline__ bool ens_chunk_sum(double v, double *part, unsigned *ticket, int s,
+                                              int c, int nch, double &total) {
+  __shared__ bool s_last;
+  double a[1] = {v};
+  block_sum<1>(a);
+  if (threadIdx.x == 0) {
+    __stcg(part + (size_t)s * gridDim.y + c, a[0]);
+    __threadfence();
+    s_last = atomicAdd(ticket + s, 1u) == (unsigned)(nch - 1);
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return false;
+  __threadfence();
+  double t = 0.0;
+  for (int q = 0; q < nch; q++) t += __ldcg(part + (size_t)s * gridDim.y + q);
+  total = t;
+  ticket[s] = 0u;
+  return true;
+}
+
+// w -= beta_{i-1} v_{i-1};  alpha_i = w . v_i
+template <class R>
+__global__ void ens_step_alpha(R *w, const R *V, size_t ldv, const int *iter, const int *off3,
+                               const int *nn, const int *active, const double *beta,
+                               double *alpha, int lim, double *part, unsigned *ticket) {
   const int s = blockIdx.x;
   if (!active[s]) return;
-  const int i = *iter;
-  const int o = off3[s], n = nn[s];
+  const int n = nn[s], nch = (n + kEstChunk - 1) / kEstChunk, c = blockIdx.y;
+  if (c >= nch) return;
+  const int i = *iter, o = off3[s];
   R *ws = w + o;
   const R *vi = V + (size_t)i * ldv + o;
   const R *vp = i > 0 ? vi - ldv : vi;
   const R bprev = i > 0 ? (R)beta[s * lim + i - 1] : R(0);
-  double v[1] = {0.0};
-  for (int e = threadIdx.x; e < n; e += kEnsThreads) {
+  double acc = 0.0;
+  for (int e = c * kEstChunk + threadIdx.x; e < min(n, (c + 1) * kEstChunk); e += kEnsThreads) {
     R x = ws[e];
     if (i > 0) x -= bprev * vp[e];
     ws[e] = x;
-    v[0] += (double)x * (double)vi[e];
+    acc += (double)x * (double)vi[e];
   }
-  block_sum<1>(v);
-  const double al = v[0];
+  double tot;
+  if (ens_chunk_sum<R>(acc, part, ticket, s, c, nch, tot)) alpha[s * lim + i] = tot;
+}
+
+// w -= alpha_i v_i;  beta_i = |w| (0 below 1e-3 alpha_i/|z|); both to the
+// device arrays and to mapped host memory
+template <class R>
+__global__ void ens_step_beta(R *w, const R *V, size_t ldv, const int *iter, const int *off3,
+                              const int *nn, const int *active, const double *normz,
+                              const double *alpha, double *beta, int lim, double *host_ab,
+                              double *part, unsigned *ticket) {
+  const int s = blockIdx.x;
+  if (!active[s]) return;
+  const int n = nn[s], nch = (n + kEstChunk - 1) / kEstChunk, c = blockIdx.y;
+  if (c >= nch) return;
+  const int i = *iter, o = off3[s];
+  R *ws = w + o;
+  const R *vi = V + (size_t)i * ldv + o;
+  const double al = alpha[s * lim + i];
   const R alr = (R)al;
-  double b2[1] = {0.0};
-  for (int e = threadIdx.x; e < n; e += kEnsThreads) {
+  double acc = 0.0;
+  for (int e = c * kEstChunk + threadIdx.x; e < min(n, (c + 1) * kEstChunk); e += kEnsThreads) {
     const R x = ws[e] - alr * vi[e];
     ws[e] = x;
-    b2[0] += (double)x * (double)x;
+    acc += (double)x * (double)x;
   }
-  block_sum<1>(b2);
-  double b = sqrt(b2[0]);
-  if (b < 1e-3 * al / normz[s]) b = 0.0;
-  if (threadIdx.x == 0) {
-    alpha[s * lim + i] = al;
+  double tot;
+  if (ens_chunk_sum<R>(acc, part, ticket, s, c, nch, tot)) {
+    double b = sqrt(tot);
+    if (b < 1e-3 * al / normz[s]) b = 0.0;
     beta[s * lim + i] = b;
     host_ab[2 * (s * lim + i)] = al;
     host_ab[2 * (s * lim + i) + 1] = b;
   }
-  R *vn = V + (size_t)(i + 1) * ldv + o;
+}
+
+// v_{i+1} = w / beta_i, or e1 after a breakdown
+template <class R>
+__global__ void ens_step_next(const R *w, R *V, R *vcur, size_t ldv, const int *iter,
+                              const int *off3, const int *nn, const int *active,
+                              const double *beta, int lim) {
+  const int s = blockIdx.x;
+  if (!active[s]) return;
+  const int n = nn[s], nch = (n + kEstChunk - 1) / kEstChunk, c = blockIdx.y;
+  if (c >= nch) return;
+  const int i = *iter, o = off3[s];
+  const double b = beta[s * lim + i];
   const R inv = b > 0.0 ? (R)(1.0 / b) : R(0);
-  for (int e = threadIdx.x; e < n; e += kEnsThreads) {
-    const R x = b > 0.0 ? ws[e] * inv : (e == 0 ? R(1) : R(0));
+  R *vn = V + (size_t)(i + 1) * ldv + o;
+  for (int e = c * kEstChunk + threadIdx.x; e < min(n, (c + 1) * kEstChunk); e += kEnsThreads) {
+    const R x = b > 0.0 ? w[o + e] * inv : (e == 0 ? R(1) : R(0));
     vn[e] = x;
     vcur[o + e] = x;
   }
@@ -511,8 +564,8 @@ template <class R> class Ensemble final : public EnsembleBase {
   // estimate partial norms [system][chunk][2] and per-system tickets
   // (self-resetting, zeroed when allocated)
   int est_chunks_ = 1;
-  DeviceBuffer<double> est_part_;
-  DeviceBuffer<unsigned> est_ticket_;
+  DeviceBuffer<double> est_part_, step_part_;
+  DeviceBuffer<unsigned> est_ticket_, step_ticket_;
   PinnedBuffer<R> pin_;
   PinnedBuffer<int> hflags_;
   MappedBuffer<double> hab_, coef_, err_;
@@ -625,6 +678,11 @@ void Ensemble<R>::set_systems(int nsys, const int *sizes, const int *geometry,
   if (est_ticket_.count < (size_t)nsys) {
     est_ticket_.ensure(nsys);
     LMG_CUDA(cudaMemset(est_ticket_.ptr, 0, est_ticket_.count * sizeof(unsigned)));
+  }
+  step_part_.ensure((size_t)nsys * est_chunks_);
+  if (step_ticket_.count < (size_t)nsys) {
+    step_ticket_.ensure(nsys);
+    LMG_CUDA(cudaMemset(step_ticket_.ptr, 0, step_ticket_.count * sizeof(unsigned)));
   }
   auto up = [](DeviceBuffer<int> &b, const std::vector<int> &v) {
     int *d = b.ensure(v.size());
@@ -753,7 +811,8 @@ template <class R> void Ensemble<R>::build_graph(R *V, size_t ldv) {
   const std::vector<const void *> key = {V,          w_.ptr,     vcur_.ptr,   iter_.ptr,
                                          off3_.ptr,  nn_.ptr,    active_.ptr, normz_.ptr,
                                          alpha_.ptr, beta_.ptr,  hab_.device_ptr(),
-                                         pos_.ptr,   part_.ptr,  tickets_.ptr};
+                                         pos_.ptr,   part_.ptr,  tickets_.ptr,
+                                         step_part_.ptr, step_ticket_.ptr};
   if (graph_ && graph_key_ == key) return;
   drop_graph();
   cudaStream_t st = cap_;
@@ -761,10 +820,17 @@ template <class R> void Ensemble<R>::build_graph(R *V, size_t ldv) {
   LMG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   try {
     for (auto &gp : groups_) launch_group(*gp, vcur_.ptr, w_.ptr, active_.ptr, st);
-    ens_step<R><<<nsys_, kEnsThreads, 0, st>>>(w_.ptr, V, vcur_.ptr, ldv, iter_.ptr,
-                                               off3_.ptr, nn_.ptr, active_.ptr, normz_.ptr,
-                                               alpha_.ptr, beta_.ptr, kEnsLimit,
-                                               hab_.device_ptr());
+    const dim3 cg(nsys_, est_chunks_);
+    ens_step_alpha<R><<<cg, kEnsThreads, 0, st>>>(w_.ptr, V, ldv, iter_.ptr, off3_.ptr, nn_.ptr,
+                                                  active_.ptr, beta_.ptr, alpha_.ptr, kEnsLimit,
+                                                  step_part_.ptr, step_ticket_.ptr);
+    ens_step_beta<R><<<cg, kEnsThreads, 0, st>>>(w_.ptr, V, ldv, iter_.ptr, off3_.ptr, nn_.ptr,
+                                                 active_.ptr, normz_.ptr, alpha_.ptr, beta_.ptr,
+                                                 kEnsLimit, hab_.device_ptr(), step_part_.ptr,
+                                                 step_ticket_.ptr);
+    ens_step_next<R><<<cg, kEnsThreads, 0, st>>>(w_.ptr, V, vcur_.ptr, ldv, iter_.ptr,
+                                                 off3_.ptr, nn_.ptr, active_.ptr, beta_.ptr,
+                                                 kEnsLimit);
     ens_iter_inc<<<1, 1, 0, st>>>(iter_.ptr);
     LMG_CUDA(cudaGetLastError());
   } catch (...) {
@@ -885,7 +951,7 @@ void Ensemble<R>::sqrt_mdot_w(const void *dW, size_t ndW, void *U, size_t nU, do
   count_launch();
   LMG_CUDA(cudaGetLastError());
   build_graph(V, ld);
-  const int per_iter = (int)groups_.size() + 2;
+  const int per_iter = (int)groups_.size() + 4;  // groups, three step kernels, counter
   auto issue = [&](int i) {
     LMG_CUDA(cudaGraphLaunch(graph_, st));
     for (int k = 0; k < per_iter; k++) count_launch();
