@@ -86,6 +86,8 @@ def load():
         fn.argtypes = args
     lib.lmg_internal_tridiag_sqrt_e1.restype = _I
     lib.lmg_internal_tridiag_sqrt_e1.argtypes = [_VP, _VP, _I, _VP]
+    lib.lmg_internal_tridiag_sqrt_e1_quad.restype = _I
+    lib.lmg_internal_tridiag_sqrt_e1_quad.argtypes = [_VP, _VP, _I, _VP]
     lib.lmg_internal_launch_count.restype = ctypes.c_ulonglong
     lib.lmg_internal_launch_count.argtypes = []
     lib.lmg_internal_mdot_plan_override.restype = _I

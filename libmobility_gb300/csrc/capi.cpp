@@ -216,6 +216,12 @@ int lmg_internal_tridiag_sqrt_e1(const double *alpha, const double *beta, int m,
   return lmg::tridiag_sqrt_e1_host(alpha, beta, m, out);
 }
 
+// The quadrature form used by the ensembles (0, or 2: use the exact form).
+int lmg_internal_tridiag_sqrt_e1_quad(const double *alpha, const double *beta, int m,
+                                      double *out) {
+  return lmg::tridiag_sqrt_e1_quad_host(alpha, beta, m, out);
+}
+
 // Internal measurement hooks (not part of the public header): switch the
 // Lanczos phase timing on or off (either resets the sums), and read the sums
 // as out[10] = {vector_ms, vector_bytes, check_ms, check_bytes, iterations,

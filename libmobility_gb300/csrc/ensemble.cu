@@ -974,7 +974,7 @@ void Ensemble<R>::sqrt_mdot_w(const void *dW, size_t ndW, void *U, size_t nU, do
     const double *hab = hab_.ptr;
     pool_.run((int)due_list.size(), [&](int k) {
       const int q = due_list[k];
-      thread_local std::vector<double> al, be, d, e, q0, out;
+      thread_local std::vector<double> al, be, d, e, q0, out, qw;
       thread_local std::vector<double2> cs;
       thread_local std::vector<int> idx;
       al.resize(m);
@@ -983,9 +983,16 @@ void Ensemble<R>::sqrt_mdot_w(const void *dW, size_t ndW, void *U, size_t nU, do
       e.resize(m);
       q0.resize(m);
       out.resize(m);
+      qw.resize(18 * (size_t)m);
       for (int t = 0; t < m; t++) {
         al[t] = hab[2 * ((size_t)q * lim + t)];
         be[t] = hab[2 * ((size_t)q * lim + t) + 1];
+      }
+      // the quadrature form (O(nodes m), independent tridiagonal solves)
+      // unless T is not positive definite or too ill-conditioned for it
+      if (tridiag_sqrt_e1_quad(al.data(), be.data(), m, qw.data(), out.data()) == 0) {
+        for (int t = 0; t < m; t++) coef[(size_t)q * lim + t] = out[t];
+        return;
       }
       int rc = 2;
       // rotations logged: about m^2; the log grows if a case needs more

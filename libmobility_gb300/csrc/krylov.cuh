@@ -16,6 +16,7 @@
 // units; alpha/beta reach it through mapped host memory while the GPU already
 // runs the next matrix-vector product.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -382,6 +383,124 @@ inline int tridiag_sqrt_e1(const double *alpha, const double *beta, int m,
     const double a0 = out[i], a1 = out[i + 1];
     out[i] = c * a0 + s * a1;
     out[i + 1] = -s * a0 + c * a1;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// T^{1/2} e1 by quadrature, for the ensemble's many per-check solves: with
+// T symmetric positive definite,
+//   T^{-1/2} = (2/pi) int_0^inf (T + t^2 I)^{-1} dt,   T^{1/2} e1 = T T^{-1/2} e1,
+// the integral taken by the trapezoidal rule after the double-exponential
+// substitution t = exp((pi/2) sinh v) (Takahasi and Mori, 1974), on T scaled
+// so that its spectrum is centred on 1; each node is one tridiagonal solve
+// (Thomas, stable for SPD), O(m), and the nodes are independent.  Node
+// spacing and range are chosen from the condition number so that the scalar
+// rule is within 1e-13 relative of 1/sqrt(lambda) over the whole spectrum
+// (checked on a log grid; 54 to 134 nodes for kappa 1e2 to 1e8); the product
+// T (T^{-1/2} e1) adds rounding of order sqrt(kappa) eps.  Returns 0,
+// or 2 when T is not positive definite, kappa is above 1e8 or a bound fails:
+// the caller then uses the exact routine above (which gives NaN for a
+// negative eigenvalue, as the reference does).  work: 18 m doubles.
+// ---------------------------------------------------------------------------
+// number of eigenvalues of T below x (Sturm count of T - x I = L D L^T)
+inline int tridiag_count_below(const double *a, const double *b, int m, double x) {
+  int c = 0;
+  double d = 1.0;
+  for (int k = 0; k < m; k++) {
+    const double bb = k > 0 ? b[k - 1] * b[k - 1] : 0.0;
+    d = (a[k] - x) - (k > 0 ? bb / d : 0.0);
+    if (d == 0.0) d = -1e-300;  // x is an eigenvalue: count it as below
+    if (d < 0.0) c++;
+  }
+  return c;
+}
+
+inline int tridiag_sqrt_e1_quad(const double *alpha, const double *beta, int m, double *work,
+                                double *out) {
+  if (m == 1) {
+    if (!(alpha[0] > 0.0)) return 2;
+    out[0] = sqrt(alpha[0]);
+    return 0;
+  }
+  // upper bound of the spectrum (Gershgorin)
+  double hi = 0.0;
+  for (int k = 0; k < m; k++) {
+    const double r = (k > 0 ? fabs(beta[k - 1]) : 0.0) + (k + 1 < m ? fabs(beta[k]) : 0.0);
+    hi = fmax(hi, alpha[k] + r);
+  }
+  if (!(hi > 0.0) || !std::isfinite(hi)) return 2;
+  if (tridiag_count_below(alpha, beta, m, 0.0) > 0) return 2;
+  // lower bound of the spectrum: step down by 4 until nothing lies below
+  double lo = hi;
+  while (tridiag_count_below(alpha, beta, m, lo) > 0) {
+    lo *= 0.25;
+    if (lo < hi * 1e-8) return 2;
+  }
+  const double kappa = hi / lo;
+  double h, vmax;
+  if (kappa <= 1e2) {
+    h = 0.15;
+    vmax = 4.0;
+  } else if (kappa <= 1e4) {
+    h = 0.1;
+    vmax = 4.0;
+  } else if (kappa <= 1e6) {
+    h = 0.08;
+    vmax = 4.5;
+  } else {
+    h = 0.06;
+    vmax = 4.0;
+  }
+  const double s = sqrt(lo * hi), is = 1.0 / s;
+  const int half = (int)(vmax / h + 0.5);
+  // work: acc[m], then 8 nodes at a time: cp[8][m], gp[8][m]
+  double *acc = work, *cp = work + m, *gp = work + 9 * m;
+  for (int k = 0; k < m; k++) acc[k] = 0.0;
+  constexpr double kPi = 3.14159265358979323846;
+  for (int j0 = -half; j0 <= half; j0 += 8) {
+    const int nq = (half - j0 + 1) < 8 ? (half - j0 + 1) : 8;
+    double t2[8], w[8];
+    for (int q = 0; q < nq; q++) {
+      const double v = (j0 + q) * h;
+      const double t = exp(0.5 * kPi * sinh(v));
+      t2[q] = t * t;
+      w[q] = h * cosh(v) * t;  // (2/pi) h (pi/2) cosh(v) t
+    }
+    // forward sweep of (T/s + t^2 I) g = e1, nodes interleaved
+    for (int q = 0; q < nq; q++) {
+      const double den = alpha[0] * is + t2[q];
+      const double inv = 1.0 / den;
+      cp[q * m] = beta[0] * is * inv;
+      gp[q * m] = inv;
+    }
+    for (int k = 1; k < m; k++) {
+      const double ek = beta[k - 1] * is;
+      const double ak = alpha[k] * is;
+      const double bk = k + 1 < m ? beta[k] * is : 0.0;
+      for (int q = 0; q < nq; q++) {
+        const double inv = 1.0 / (ak + t2[q] - ek * cp[q * m + k - 1]);
+        cp[q * m + k] = bk * inv;
+        gp[q * m + k] = -ek * gp[q * m + k - 1] * inv;
+      }
+    }
+    // back substitution, weighted into acc
+    for (int q = 0; q < nq; q++) {
+      double g = gp[q * m + m - 1];
+      acc[m - 1] += w[q] * g;
+      for (int k = m - 2; k >= 0; k--) {
+        g = gp[q * m + k] - cp[q * m + k] * g;
+        acc[k] += w[q] * g;
+      }
+    }
+  }
+  // T^{-1/2} e1 = s^{-1/2} acc;  out = T (s^{-1/2} acc)
+  const double f = 1.0 / sqrt(s);
+  for (int k = 0; k < m; k++) {
+    double y = alpha[k] * acc[k];
+    if (k > 0) y += beta[k - 1] * acc[k - 1];
+    if (k + 1 < m) y += beta[k] * acc[k + 1];
+    out[k] = f * y;
   }
   return 0;
 }

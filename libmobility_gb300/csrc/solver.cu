@@ -931,6 +931,12 @@ SolverBase *make_solver(Periodicity x, Periodicity y, Periodicity z, int precisi
   throw Error(LMG_ERR_INVALID_ARGUMENT, "[libmobility_gb300] precision must be 0 (float) or 1 (double)");
 }
 
+int tridiag_sqrt_e1_quad_host(const double *alpha, const double *beta, int m, double *out) {
+  if (m < 1 || m > 256) return 3;
+  std::vector<double> work(18 * (size_t)m);
+  return tridiag_sqrt_e1_quad(alpha, beta, m, work.data(), out);
+}
+
 int tridiag_sqrt_e1_host(const double *alpha, const double *beta, int m, double *out) {
   if (m < 1 || m > 256) return 3;
   std::vector<double> d(m), e(m), q(m);

@@ -136,5 +136,8 @@ SolverBase *make_self_mobility(Periodicity x, Periodicity y, Periodicity z, int 
 // internal test hook: T^{1/2} e1 for a symmetric tridiagonal matrix (FP64,
 // host build of the device solver).  Returns 0 on success.
 int tridiag_sqrt_e1_host(const double *alpha, const double *beta, int m, double *out);
+// the same by quadrature (the ensemble's routine): 0, or 2 when the caller
+// must fall back to the exact one
+int tridiag_sqrt_e1_quad_host(const double *alpha, const double *beta, int m, double *out);
 
 }  // namespace lmg

@@ -194,3 +194,71 @@ def test_tridiagonal_negative_eigenvalue_gives_nan(lib):
     out = np.zeros(3)
     lib.lmg_internal_tridiag_sqrt_e1(a.ctypes.data, b.ctypes.data, 3, out.ctypes.data)
     assert np.isnan(out).any()
+
+
+def _lanczos_tridiagonal(lam, m, rng):
+    """Lanczos (full reorthogonalisation) on a matrix with spectrum lam."""
+    n = len(lam)
+    Q, _ = np.linalg.qr(rng.normal(size=(n, n)))
+    A = Q @ np.diag(lam) @ Q.T
+    v = rng.normal(size=n)
+    V = [v / np.linalg.norm(v)]
+    al, be = [], []
+    for k in range(m):
+        w = A @ V[-1]
+        al.append(V[-1] @ w)
+        for u in V:
+            w -= (u @ w) * u
+        if k == m - 1:
+            break
+        be.append(np.linalg.norm(w))
+        V.append(w / be[-1])
+    return np.array(al), np.array(be)
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 7, 50, 120, 200])
+def test_tridiagonal_sqrt_e1_quadrature(lib, m):
+    """The ensembles' quadrature form of T^{1/2} e1 against the eigen-solution."""
+    rng = np.random.default_rng(100 + m)
+    a = rng.uniform(1.0, 3.0, m)
+    b = rng.uniform(-0.4, 0.4, m)
+    out = np.zeros(m)
+    assert lib.lmg_internal_tridiag_sqrt_e1_quad(a.ctypes.data, b.ctypes.data, m,
+                                                 out.ctypes.data) == 0
+    ref = _tridiag_sqrt_reference(a, b[: m - 1])
+    assert np.linalg.norm(out - ref) <= 1e-13 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e4, 1e6, 1e7])
+def test_tridiagonal_quadrature_condition_numbers(lib, kappa):
+    """Spectra over [1, kappa] with a cluster, as Lanczos produces.  The rule
+    itself is within 1e-13 of 1/sqrt(lambda); the product T (T^{-1/2} e1)
+    adds rounding of order sqrt(kappa) eps, so the bound grows with kappa.
+    (The condition number is bounded from above by Gershgorin and a Sturm
+    search in factors of 4, so a true kappa of ~1e7 already meets the 1e8
+    limit of the node sets.)"""
+    rng = np.random.default_rng(int(np.log10(kappa)))
+    lam = np.concatenate([np.logspace(0, np.log10(kappa), 50), np.full(10, 2.0)])
+    a, b = _lanczos_tridiagonal(lam, 60, rng)
+    out = np.zeros(60)
+    assert lib.lmg_internal_tridiag_sqrt_e1_quad(a.ctypes.data, b.ctypes.data, 60,
+                                                 out.ctypes.data) == 0
+    ref = _tridiag_sqrt_reference(a, b)
+    bound = 1e-13 * max(1.0, np.sqrt(kappa) / 100)
+    assert np.linalg.norm(out - ref) <= bound * np.linalg.norm(ref)
+
+
+def test_tridiagonal_quadrature_defers_to_exact_form(lib):
+    """Not positive definite, or beyond kappa = 1e8: return 2 (the caller
+    then takes the exact routine, which gives NaN for a negative eigenvalue)."""
+    out = np.zeros(3)
+    a, b = np.array([1.0, -2.0, 1.0]), np.array([0.1, 0.1])
+    assert lib.lmg_internal_tridiag_sqrt_e1_quad(a.ctypes.data, b.ctypes.data, 3,
+                                                 out.ctypes.data) == 2
+    a1 = np.array([-1.0])
+    assert lib.lmg_internal_tridiag_sqrt_e1_quad(a1.ctypes.data, b.ctypes.data, 1,
+                                                 out.ctypes.data) == 2
+    a, b = _lanczos_tridiagonal(np.logspace(0, 11, 40), 40, np.random.default_rng(7))
+    out = np.zeros(40)
+    assert lib.lmg_internal_tridiag_sqrt_e1_quad(a.ctypes.data, b.ctypes.data, 40,
+                                                 out.ctypes.data) == 2
