@@ -25,6 +25,7 @@ UNITS = [
     ("mdot_launch.cu", ["-DLMG_REAL=float"], "mdot_f.o"),
     ("mdot_launch.cu", ["-DLMG_REAL=double"], "mdot_d.o"),
     ("solver.cu", [], "solver.o"),
+    ("mdot_sym.cu", [], "mdot_sym.o"),
     ("probes.cu", [], "probes.o"),
     ("noalloc.cu", [], "noalloc.o"),
     ("precond.cu", [], "precond.o"),

@@ -96,6 +96,10 @@ def load():
     lib.lmg_internal_fma_probe.argtypes = [_I, _I, _I, _VP, _VP]
     lib.lmg_internal_fma2_probe.restype = _I
     lib.lmg_internal_fma2_probe.argtypes = [_I, _I, _I, _VP, _VP]
+    lib.lmg_internal_dfma_probe.restype = _I
+    lib.lmg_internal_dfma_probe.argtypes = [_I, _I, _I, _VP, _VP]
+    lib.lmg_internal_sym_plan.restype = _I
+    lib.lmg_internal_sym_plan.argtypes = [_I, _I, ctypes.c_longlong, _I, _VP, _VP, _VP, _VP, _VP]
     _F = ctypes.c_float
     internal = {
         "lmg_internal_gemm": [_I, _I, _I, _I, _I, _VP, _I, _VP, _I, _VP, _I, _VP, _I, _F, _VP],
@@ -113,6 +117,8 @@ def load():
         "lmg_internal_lanczos_phase_timing": [_VP, _I],
         "lmg_internal_lanczos_phase_times": [_VP, _VP],
         "lmg_internal_barrier_timeout_probe": [_VP],
+        "lmg_internal_sym_override": [_I, _I],
+        "lmg_internal_sym_trace": [_VP],
     }
     for name, args in internal.items():
         fn = getattr(lib, name)

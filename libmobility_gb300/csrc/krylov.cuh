@@ -20,6 +20,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "grid_sync.cuh"
+
 namespace lmg {
 
 // ---------------------------------------------------------------------------
@@ -199,38 +201,6 @@ __global__ void krylov_scale_first_kernel(const R *z, R *v0, size_t n, const Kry
 // (mapped host memory, read by the host at its next check) and returns; the
 // host resets the barrier words before every solve.
 // ---------------------------------------------------------------------------
-constexpr long kBarrierSpins = 1L << 24;  // x >= 64 ns sleep: > 1 s
-
-// bar[0] arrivals, bar[1] generation.  Returns false if the wait ran out.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned *gen = bar + 1;
-    const unsigned g = *gen;
-    __threadfence();
-    int ok = 1;
-    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      ok = 0;
-      for (long it = 0; it < kBarrierSpins; it++) {
-        if (*gen != g) {
-          ok = 1;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
 template <class R>
 __global__ void __launch_bounds__(kRedThreads)
 krylov_step_kernel(R *w, const R *vi, const R *vprev, R *vnext, size_t n, int i,

@@ -9,4 +9,10 @@ extern std::atomic<unsigned long long> g_launches;
 inline void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 // 0 = planner's choice
 extern std::atomic<int> g_force_tpt, g_force_split;
+// symmetric open-space product: g_sym_mode 0 = used where it applies, 1 = off;
+// g_sym_warps > 0 caps the warps its steps are spread over; g_sym_variant is
+// its register budget, 2, 3 or 4 resident blocks per SM (0 = default, 2)
+extern std::atomic<int> g_sym_mode, g_sym_warps, g_sym_variant;
+// device buffer for the symmetric kernel's timeline (null = off)
+extern std::atomic<unsigned long long *> g_sym_trace;
 }  // namespace lmg

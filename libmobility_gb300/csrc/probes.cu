@@ -8,15 +8,19 @@
 //     up and reports instead of waiting forever.
 #include <atomic>
 #include <cstdint>
+#include <cstring>
 
 #include <cuda_runtime.h>
 
 #include "krylov.cuh"
 #include "launch_count.hpp"
+#include "mdot_sym.cuh"
 
 namespace lmg {
 std::atomic<unsigned long long> g_launches{0};
 std::atomic<int> g_force_tpt{0}, g_force_split{0};
+std::atomic<int> g_sym_mode{0}, g_sym_warps{0}, g_sym_variant{0};
+std::atomic<unsigned long long *> g_sym_trace{nullptr};
 }
 
 namespace {
@@ -60,6 +64,25 @@ __global__ void fma2_chain_kernel(int iters, float *sink) {
   if (s == -1.0f) sink[threadIdx.x] = s;
 }
 
+// FP64: 8 independent DFMA chains per thread, the same structure.
+__global__ void dfma_chain_kernel(int iters, double *sink) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) a[k] = (threadIdx.x + k) * 1e-7;
+  const double b = 0.999999, c = 1e-8;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) a[k] = fma(a[k], b, c);
+    }
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += a[k];
+  if (s == -1.0) sink[threadIdx.x] = s;
+}
+
 // Two blocks meet at a barrier whose arrival count starts at 7: neither is
 // the last arrival, nothing advances the generation word, so both waits run
 // out and report.
@@ -82,6 +105,62 @@ int lmg_internal_mdot_plan_override(int tpt, int nsplit) {
   return 0;
 }
 
+// Symmetric open-space product of FP32 handles: mode 0 uses it wherever it
+// applies (open boundary, forces only, no angular part, 16-byte aligned
+// forces, batches of a multiple of 4 particles or a single batch), mode 1
+// always takes mdot_kernel; warps > 0 caps the number of warps its rotation
+// steps are spread over (tests cut tile pairs at many places with it).
+// Modes 2, 3 and 4 instead pick the kernel build for 2, 3 or 4 resident
+// blocks per SM (register budget), leaving the rest as it is.  Applies to the
+// next product of every handle.
+int lmg_internal_sym_override(int mode, int warps) {
+  if (mode < 0 || mode > 4 || warps < 0) return 1;
+  if (mode >= 2) {
+    lmg::g_sym_variant.store(mode);
+    return 0;
+  }
+  lmg::g_sym_mode.store(mode);
+  lmg::g_sym_warps.store(warps);
+  return 0;
+}
+
+// Host tables of the symmetric kernel's schedule for `resident` resident
+// blocks (no device needed).  info[0..8] receives nwarps, tile pairs, tiles,
+// slots, threads per element of the fold, blocks, rotation steps, tiles per
+// batch and slots per tile; the arrays (pairs: 4 ints per pair, pseg: 1 per
+// pair, warps: 8 per warp, tused: 1 per tile) are filled when not null.
+// Returns 0, or 2 when the shape does not suit the kernel.
+int lmg_internal_sym_plan(int N, int nper, long long resident, int force_warps, long long *info,
+                          int *pairs, int *pseg, int *warps, int *tused) {
+  lmg::SymPlan p;
+  const cudaError_t e = lmg::mdot_sym_plan_tables(N, nper, resident, force_warps, p);
+  if (e == cudaErrorNotSupported) return 2;
+  if (e != cudaSuccess || !info) return 1;
+  info[0] = p.nwarps;
+  info[1] = (long long)p.pairs.size();
+  info[2] = (long long)p.tused.size();
+  info[3] = (long long)p.slots;
+  info[4] = p.rt;
+  info[5] = p.grid;
+  info[6] = p.steps;
+  info[7] = p.tpb;
+  info[8] = p.cmax;
+  if (pairs) std::memcpy(pairs, p.pairs.data(), p.pairs.size() * sizeof(int4));
+  if (pseg) std::memcpy(pseg, p.pseg.data(), p.pseg.size() * sizeof(int));
+  if (warps) std::memcpy(warps, p.warps.data(), p.warps.size() * sizeof(int4));
+  if (tused) std::memcpy(tused, p.tused.data(), p.tused.size() * sizeof(int));
+  return 0;
+}
+
+// Timeline of the next symmetric-kernel launches (measurement hook, off when
+// null): `buf` is device memory of 2 * (warps + blocks) 64-bit words, filled
+// with %globaltimer nanoseconds: per warp its start and the end of its
+// rotation steps, then per block the end of the grid barrier and of the fold.
+int lmg_internal_sym_trace(void *buf) {
+  lmg::g_sym_trace.store(static_cast<unsigned long long *>(buf));
+  return 0;
+}
+
 // Launches blocks x threads of the FMA chain on `stream`; flops performed =
 // blocks * threads * iters * 64 * 2.
 int lmg_internal_fma_probe(int blocks, int threads, int iters, void *sink, void *stream) {
@@ -92,6 +171,12 @@ int lmg_internal_fma_probe(int blocks, int threads, int iters, void *sink, void 
 // Packed variant: the same flop count as lmg_internal_fma_probe.
 int lmg_internal_fma2_probe(int blocks, int threads, int iters, void *sink, void *stream) {
   fma2_chain_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, (float *)sink);
+  return (int)cudaGetLastError();
+}
+
+// FP64 variant: flops performed = blocks * threads * iters * 64 * 2.
+int lmg_internal_dfma_probe(int blocks, int threads, int iters, void *sink, void *stream) {
+  dfma_chain_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, (double *)sink);
   return (int)cudaGetLastError();
 }
 

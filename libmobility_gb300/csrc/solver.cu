@@ -8,15 +8,19 @@
 //   clean          MobilityInterface.h:220-223
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <limits>
 #include <map>
+#include <memory>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
 #include "krylov.cuh"
 #include "launch_count.hpp"
 #include "mdot_launch.cuh"
+#include "mdot_sym.cuh"
 #include "precond.cuh"
 #include "solver.hpp"
 
@@ -164,6 +168,21 @@ template <class R> class Solver final : public SolverBase {
   int step_per_sm_ = 0;  // resident krylov_step_kernel blocks per SM
   bool tickets_zeroed_ = false;
   std::map<long, MdotPlan> plans_;
+  // symmetric open-space product (FP32): plans with their device tables,
+  // partial sums and barrier counts, and the flag a barrier that timed out
+  // raises
+  struct SymState {
+    SymPlan plan;
+    DeviceBuffer<int4> pairs, warps;
+    DeviceBuffer<int> pseg;
+    // arrival count of the kernel's grid barrier: one per plan, so every
+    // launch that uses it has the same block count
+    DeviceBuffer<unsigned long long> count;
+    DeviceBuffer<float> part;  // partial sums (slots nobody writes stay zero)
+  };
+  std::map<std::tuple<int, int, int, int>, std::unique_ptr<SymState>> sym_plans_;
+  MappedBuffer<int> sym_err_;
+  bool mdot_sym(const R *pos, const R *F, R *U);
 
   void release_all();
   int sms();
@@ -201,6 +220,8 @@ template <class R> void Solver<R>::release_all() {
   cvec_.release(); mirror_.release(); hc_.release(); ql_work_ = {}; rot_cs_ = {}; rot_idx_ = {};
   h_dbl_.release(); rfd_noise_.release(); rfd_pos_.release(); rfd_mp_.release(); rfd_mm_.release();
   plans_.clear();
+  sym_plans_.clear();
+  sym_err_.release();
   tickets_zeroed_ = false;
 }
 
@@ -303,6 +324,7 @@ void Solver<R>::mdot_device(const R *pos, const R *F, const R *T, R *U, R *W) {
     if (W) LMG_CUDA(cudaMemsetAsync(W, 0, 3 * (size_t)N * sizeof(R), stream()));
     return;
   }
+  if (s.geom == kOpen && s.has_f && !s.has_t && !s.ang && mdot_sym(pos, F, U)) return;
   const int ftpt = g_force_tpt.load(), fsplit = g_force_split.load();
   const long key = ((long)N << 30) | ((long)fsplit << 10) | (ftpt << 8) | (s.geom << 3) |
                    (s.has_f << 2) | (s.has_t << 1) | s.ang;
@@ -340,6 +362,70 @@ void Solver<R>::mdot_device(const R *pos, const R *F, const R *T, R *U, R *W) {
   a.part = part_.ptr;
   a.ticket = tickets_.ptr;
   LMG_CUDA(mdot_launch<R>(s, a, plan, stream()));
+}
+
+// U = M F with the symmetric open-space kernel (FP32, forces only, no
+// angular part): returns false where that kernel does not apply.
+template <class R> bool Solver<R>::mdot_sym(const R *pos, const R *F, R *U) {
+  if constexpr (!std::is_same_v<R, float>) {
+    return false;
+  } else {
+    if (g_sym_mode.load() != 0 || U == nullptr) return false;
+    if ((reinterpret_cast<uintptr_t>(F) | reinterpret_cast<uintptr_t>(pos)) & 15) return false;
+    const int N = (int)N_;
+    const int warps = g_sym_warps.load();
+    const auto key = std::make_tuple(N, batch_size(), warps, g_sym_variant.load());
+    auto it = sym_plans_.find(key);
+    if (it == sym_plans_.end()) {
+      auto st = std::make_unique<SymState>();
+      const cudaError_t e = mdot_sym_plan(N, batch_size(), sms(), warps, st->plan);
+      if (e != cudaSuccess && e != cudaErrorNotSupported) LMG_CUDA(e);
+      if (e != cudaSuccess) {
+        st->plan.grid = 0;
+      } else {
+        const SymPlan &p = st->plan;
+        auto up = [&](auto &buf, const auto &v) {
+          buf.ensure(v.size());
+          LMG_CUDA(cudaMemcpyAsync(buf.ptr, v.data(), v.size() * sizeof(v[0]),
+                                   cudaMemcpyHostToDevice, stream()));
+        };
+        up(st->pairs, p.pairs);
+        up(st->pseg, p.pseg);
+        up(st->warps, p.warps);
+        st->count.ensure(1);
+        LMG_CUDA(cudaMemsetAsync(st->count.ptr, 0, sizeof(unsigned long long), stream()));
+        st->part.ensure(p.part_elems);
+        LMG_CUDA(cudaMemsetAsync(st->part.ptr, 0, p.part_elems * sizeof(float), stream()));
+        // the host tables must outlive the copies
+        LMG_CUDA(cudaStreamSynchronize(stream()));
+      }
+      it = sym_plans_.insert_or_assign(key, std::move(st)).first;
+    }
+    const SymState &st = *it->second;
+    const SymPlan &p = st.plan;
+    if (p.grid <= 0) return false;
+    if (!sym_err_.ptr) sym_err_.ensure(1);
+    if (*(volatile int *)sym_err_.ptr) {
+      // a barrier wait ran out in an earlier launch: arrival counts are
+      // inconsistent, start them afresh
+      LMG_CUDA(cudaStreamSynchronize(stream()));
+      for (auto &kv : sym_plans_)
+        if (kv.second->count.ptr)
+          LMG_CUDA(cudaMemsetAsync(kv.second->count.ptr, 0, sizeof(unsigned long long),
+                                   stream()));
+      *(volatile int *)sym_err_.ptr = 0;
+      throw Error(LMG_ERR_TIMEOUT,
+                  "[libmobility_gb300] Mdot: grid barrier of the symmetric kernel timed out");
+    }
+    const PairConst<float> k = make_pair_const<float>(t0_, r0_, rt0_);
+    SymTables tab;
+    tab.pairs = st.pairs.ptr;
+    tab.pseg = st.pseg.ptr;
+    tab.warps = st.warps.ptr;
+    LMG_CUDA(mdot_sym_launch(p, tab, pos, F, U, (float)(1.0 / a_), k, st.part.ptr, st.count.ptr,
+                             sym_err_.device_ptr(), stream()));
+    return true;
+  }
 }
 
 template <class R>
