@@ -196,6 +196,200 @@ def fp32_peak_tflops(lib, torch):
     return best
 
 
+def fp64_peak_tflops(lib, torch):
+    """FP64 FMA throughput of this GPU, measured now (same structure as the
+    FP32 probe; GB300's FP64 units are narrow, so fewer rounds)."""
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 128
+    sink = torch.zeros(threads, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    lib.lmg_internal_dfma_probe(blocks, threads, iters, sink.data_ptr(), st)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lib.lmg_internal_dfma_probe(blocks, threads, iters, sink.data_ptr(), st)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        best = max(best, blocks * threads * iters * 64 * 2 / t / 1e12)
+    return best
+
+
+def graph_time(torch, fn, reps=20):
+    """Average device time of `fn` (one kernel launch, or a few) captured
+    `reps` times in a CUDA graph and replayed between CUDA events, so the host
+    cost of the Python call does not starve the GPU at small sizes; without
+    graph capture, back-to-back calls are timed."""
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    try:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, capture_error_mode="relaxed"):
+            for _ in range(reps):
+                fn()
+        g.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.replay()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / reps, "cuda-graph replay of %d launches" % reps
+    except Exception as exc:  # pragma: no cover - depends on the driver
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / reps, f"back-to-back calls ({exc.__class__.__name__})"
+
+
+def flushed_time(torch, fn, flush, reps=20):
+    """Median device time of one call of `fn` right after the L2 is flushed
+    (its inputs then come from HBM), CUDA events around the call."""
+    ts = []
+    for _ in range(reps):
+        flush_l2(flush)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    return statistics.median(ts)
+
+
+def config1_inputs(seed=1234):
+    """N = 4096 uniform in the cube of volume fraction 0.05 (a = 1), forces
+    N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    N = 4096
+    L = (N * 4 * math.pi / 3 / 0.05) ** (1 / 3)
+    return rng.uniform(0, L, (N, 3)), rng.normal(size=(N, 3))
+
+
+def open4k_mdot(torch, lib, peak32, peak64, flush):
+    """Configuration 1: open-boundary translational Mdot, N = 4096, a = 1,
+    viscosity 1/(6 pi), in FP32 and FP64 on device-resident inputs.  The FP32
+    handle takes the symmetric kernel; the tiled kernel's time on the same
+    handle is given beside it.  Returns the sub-object and the results (for
+    the error against the FP64 oracle, filled in by the caller)."""
+    from libmobility_gb300 import NBody
+    pos, F = config1_inputs()
+    N = pos.shape[0]
+    pairs = float(N) * N
+    out = {"workload": "open RPY (UF), N=4096, cube at phi=0.05, a=1, viscosity 1/(6 pi), "
+                       "F ~ N(0,1), seed 1234",
+           "pairs": pairs, "flops_per_pair": FLOPS_PER_PAIR[("open", False)]}
+    results = {}
+    for prec, dt, peak in (("float", torch.float32, peak32), ("double", torch.float64, peak64)):
+        s = NBody("open", "open", "open", precision=prec)
+        s.setParameters()
+        s.initialize(viscosity=1 / (6 * math.pi), hydrodynamicRadius=1.0)
+        dpos = torch.tensor(pos, dtype=dt, device="cuda")
+        dF = torch.tensor(F, dtype=dt, device="cuda")
+        s.setPositions(dpos)
+        t, how = graph_time(torch, lambda: s.Mdot(dF, None), reps=50)
+        t_cold = flushed_time(torch, lambda: s.Mdot(dF, None), flush)
+        U, _ = s.Mdot(dF, None)
+        torch.cuda.synchronize()
+        results[prec] = U.double().cpu().numpy()
+        ach = pairs * out["flops_per_pair"] / t / 1e12
+        e = {"ms": t * 1e3, "pair_interactions_per_s": pairs / t, "achieved_tflops": ach,
+             "peak_tflops": peak, "frac": ach / peak,
+             "peak_source": ("FP32" if prec == "float" else "FP64") + " FMA-chain probe "
+                            "measured in this run",
+             "kernel_timing": how + " (inputs in L2)",
+             "ms_after_l2_flush": t_cold * 1e3}
+        if prec == "float":
+            e["kernel"] = "mdot_sym_kernel (symmetric, each unordered pair once)"
+            assert lib.lmg_internal_sym_override(1, 0) == 0
+            try:
+                t_tiled, _ = graph_time(torch, lambda: s.Mdot(dF, None), reps=50)
+            finally:
+                lib.lmg_internal_sym_override(0, 0)
+            e["tiled_kernel_ms"] = t_tiled * 1e3
+            e["speedup_vs_tiled_kernel"] = t_tiled / t
+        else:
+            e["kernel"] = "mdot_kernel<double>"
+        out[prec] = e
+    return out, pos, F, results
+
+
+def reference_gpu_mdot(torch, wall16k_inputs):
+    """libMobility's own NBody CUDA kernel (computeRPYBatchedFastGPU, launch
+    shape of its launcher, NbodyRPY.cu:99-116), compiled for sm_103a from the
+    reference sources into oracle/_ref, next to this library's Mdot on the
+    same GPU and inputs: configuration 1 (open UF, N = 4096) and configuration
+    2 (single wall, all blocks, N = 16384), FP32 and FP64, both timed as CUDA
+    graph replays of 20 launches on device buffers."""
+    import ctypes
+    from oracle import build as ob
+    from libmobility_gb300 import NBody
+    ob.build_oracle()
+    here = ROOT / "oracle"
+    cubins = [here / "_ref" / f"ref_nbody_{t}.cubin" for t in ("f", "d")]
+    if not all(c.exists() for c in cubins):
+        return {"unavailable": "reference cubin not built (oracle/_ref is made where the "
+                               "reference sources are)"}
+    rl = ctypes.CDLL(str(here / "_build" / "libref_gpu_launcher.so"))
+    rl.ref_gpu_last_error.restype = ctypes.c_char_p
+    for dbl, c in enumerate(cubins):
+        if rl.ref_gpu_load(dbl, str(c).encode()):
+            return {"unavailable": rl.ref_gpu_last_error().decode()}
+    a, eta = 1.0, 1 / (6 * math.pi)
+    t0, r0, rt0 = 1 / (6 * math.pi * eta * a), 1 / (8 * math.pi * eta * a ** 3), \
+        1 / (8 * math.pi * eta * a * a)
+    pos1, F1 = config1_inputs()
+    pos2, F2, T2, _ = wall16k_inputs
+    out = {"kernel": "computeRPYBatchedFastGPU (libMobility NbodyRPY.cu:26-97), sm_103a cubin"}
+    for name, wall, ang, pos, F, T, fpp in (
+            ("open4k_uf", 0, 0, pos1, F1, None, FLOPS_PER_PAIR[("open", False)]),
+            ("wall16k_6x6", 1, 1, pos2, F2, T2, FLOPS_PER_PAIR[("wall", True)])):
+        N = pos.shape[0]
+        ent = {}
+        for prec, dt in (("float", torch.float32), ("double", torch.float64)):
+            dp = torch.tensor(pos, dtype=dt, device="cuda")
+            dF = torch.tensor(F, dtype=dt, device="cuda")
+            dT = torch.tensor(T, dtype=dt, device="cuda") if T is not None else None
+            U = torch.zeros((N, 3), dtype=dt, device="cuda")
+            W = torch.zeros((N, 3), dtype=dt, device="cuda")
+
+            def ref():
+                st = torch.cuda.current_stream().cuda_stream
+                rc = rl.ref_gpu_mdot(ctypes.c_int(prec == "double"), ctypes.c_int(wall),
+                                     ctypes.c_void_p(dp.data_ptr()),
+                                     ctypes.c_void_p(dF.data_ptr()),
+                                     ctypes.c_void_p(dT.data_ptr() if dT is not None else None),
+                                     ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(W.data_ptr()),
+                                     ctypes.c_int(1), ctypes.c_int(N), ctypes.c_double(t0),
+                                     ctypes.c_double(r0), ctypes.c_double(rt0), ctypes.c_double(a),
+                                     ctypes.c_int(ang), ctypes.c_void_p(st))
+                if rc:
+                    raise RuntimeError(rl.ref_gpu_last_error().decode())
+
+            t_ref, _ = graph_time(torch, ref)
+            s = NBody("open", "open", "single_wall" if wall else "open", precision=prec)
+            s.setParameters(**({"wallHeight": 0.0} if wall else {}))
+            s.initialize(viscosity=eta, hydrodynamicRadius=a, includeAngular=bool(ang))
+            s.setPositions(dp)
+            t_me, _ = graph_time(torch, lambda: s.Mdot(dF, dT))
+            pairs = float(N) * N
+            ent[prec] = {"reference_ms": t_ref * 1e3, "ours_ms": t_me * 1e3,
+                         "reference_pair_interactions_per_s": pairs / t_ref,
+                         "ours_pair_interactions_per_s": pairs / t_me,
+                         "reference_tflops": pairs * fpp / t_ref / 1e12,
+                         "speedup": t_ref / t_me}
+        out[name] = ent
+    out["timing"] = "cuda-graph replay of 20 launches each, device buffers, inputs in L2"
+    return out
+
+
 def mdot_kernel_time(torch, s, dF, dT, reps=20):
     """Average time of one Mdot launch on the device.  The launches are
     captured in a CUDA graph and replayed between CUDA events on the same
@@ -504,6 +698,19 @@ def cpu_baseline(w, pos, F, T, seconds=8.0):
             "sample": f"FP64 C oracle, Mdot rows 0..{rows - 1} x {N} sources, {reps} reps"}
 
 
+def oracle_error_open4k(pos, F, results):
+    """Max |U - U_oracle| / max |U_oracle| of the configuration-1 products
+    against the FP64 C oracle (all host threads), every row."""
+    from oracle import build as ob
+    ob.build_oracle()
+    from oracle import oracle as orc
+    Uo, _ = orc.mdot(pos, F, None, a=1.0, viscosity=1 / (6 * math.pi), wall=0,
+                     include_angular=0, nthreads=os.cpu_count() or 1)
+    Uo = np.asarray(Uo, np.float64).reshape(-1)
+    scale = np.abs(Uo).max()
+    return {p: float(np.abs(u.reshape(-1) - Uo).max() / scale) for p, u in results.items()}
+
+
 def run_reference(args, w, ws, rank):
     if rank != 0:
         return
@@ -591,6 +798,11 @@ def run_ours(args, w, ws, rank, local):
     t_sqrt = (time.perf_counter() - t0) / 3
     krylov = krylov_phases(torch, s, ddW, t_mdot)
     peak = fp32_peak_tflops(lib, torch)
+    peak64 = fp64_peak_tflops(lib, torch)
+    open4k, pos1, F1, res1 = open4k_mdot(torch, lib, peak, peak64, flush)
+    ref_gpu = None
+    if not args.skip_reference_gpu:
+        ref_gpu = reference_gpu_mdot(torch, (pos, F, T, dW))
     fpp = FLOPS_PER_PAIR[("wall" if w["wall"] else "open", w["ang"])]
     achieved = pairs * fpp / t_mdot / 1e12
 
@@ -643,6 +855,11 @@ def run_ours(args, w, ws, rank, local):
     if rank != 0:
         return
     cpu = cpu_baseline(w, pos, F, T)
+    err1 = oracle_error_open4k(pos1, F1, res1)
+    for prec, e in err1.items():
+        open4k[prec]["max_rel_err_vs_fp64_oracle"] = e
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    datasheet = (sms * 256 * clocks["sm_mhz"] * 1e-6) if clocks else None
     line = {
         "metric": METRIC, "value": value, "unit": "pair-interactions/s", "n_gpus": ws,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": t_step * 1e3,
@@ -656,6 +873,8 @@ def run_ours(args, w, ws, rank, local):
         "sqrtMdotW_learned_vs_plain": cmp,
         "ensemble_256": ens,
         "wall_262k_mdot": large,
+        "open4k_mdot": open4k,
+        "reference_gpu": ref_gpu,
         "krylov_phases": krylov,
         "mdot_pair_interactions_per_s": pairs / t_mdot,
         "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "h2d_bytes_per_step": h2d,
@@ -666,6 +885,9 @@ def run_ours(args, w, ws, rank, local):
                      "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one "
                                        "ncu capture of this kernel and workload",
                      "peak_source": "FP32 FMA-chain probe measured in this run",
+                     "datasheet_fp32_tflops": datasheet,
+                     "datasheet_note": "SMs x 128 FP32 FMA/clk x 2 flops x median SM clock "
+                                       "under load",
                      "flops_per_pair": fpp, "kernel_ms": t_mdot * 1e3,
                      "kernel_timing": kernel_timing},
         "cpu_baseline": cpu,
@@ -688,7 +910,9 @@ def main():
                     help="skip the batched ensemble of 256 uneven systems")
     ap.add_argument("--skip-large", action="store_true",
                     help="skip the N = 262144 single-wall Mdot")
-    ap.add_argument("--only", choices=["ensemble", "precond"], default=None,
+    ap.add_argument("--skip-reference-gpu", action="store_true",
+                    help="skip the reference CUDA kernel timed beside this library's Mdot")
+    ap.add_argument("--only", choices=["ensemble", "precond", "open4k"], default=None,
                     help="run one sub-measurement alone and print it (for profiling)")
     ap.add_argument("--ensemble-systems", type=int, default=256)
     args = ap.parse_args()
@@ -706,6 +930,16 @@ def main():
         out = sqrtmdotw_comparison(torch, args.steps, args.warmup, rank)
         if rank == 0:
             print(json.dumps({"sqrtMdotW_learned_vs_plain": out}))
+        return
+    if args.only == "open4k":  # configuration 1 alone (profiling runs)
+        import torch
+        from libmobility_gb300 import _capi
+        lib = _capi.load()
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        out, _, _, _ = open4k_mdot(torch, lib, fp32_peak_tflops(lib, torch),
+                                   fp64_peak_tflops(lib, torch), flush)
+        if rank == 0:
+            print(json.dumps({"open4k_mdot": out}))
         return
     if args.impl == "reference":
         run_reference(args, w, ws, rank)
