@@ -199,13 +199,17 @@ const char *lmg_precision_name(const lmg_solver *h);
  * cannot take the device-wide synchronisation of cudaMalloc/cudaFree.  No
  * handle: every input and output is a caller-owned DEVICE buffer of 3N floats
  * (positions measured from the wall, z = 0 at the wall, when single_wall;
- * no below-the-wall check is made); F or T may be NULL, W is required with
- * includeAngular; U and W are overwritten as by lmg_mdot.  NperBatch <= 0
+ * no below-the-wall check is made); one of F and T may be NULL (not both: a
+ * call without forces and torques is rejected), W is required with
+ * includeAngular; U and W are overwritten as by lmg_mdot.  Buffers must live
+ * on the current GPU.  NperBatch <= 0
  * means one batch.  The kernel's scratch is a static device array of
  * LMG_MDOT_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library;
- * numberParticles above LMG_MDOT_NOALLOC_MAX_PARTICLES is rejected.  The first
- * call on a device sets up the scratch address (make it before any stream
- * capture); calls share the scratch, so calls that overlap on the GPU race.
+ * numberParticles above LMG_MDOT_NOALLOC_MAX_PARTICLES is rejected.  Every call
+ * looks up the scratch address on the current device; the first call on a
+ * device also loads the library's device code there (make it before any
+ * stream capture); calls share the scratch, so calls that overlap on the GPU
+ * race.
  * Work is issued on cuda_stream (0 = default stream), nothing is synchronised.
  * On failure a message is written to err (err_len bytes, may be NULL). */
 #define LMG_MDOT_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)

@@ -31,6 +31,38 @@ struct Error : std::runtime_error {
     if (lmg_e_ != cudaSuccess) ::lmg::throw_cuda(lmg_e_, #call); \
   } while (0)
 
+// Where a caller's buffer lives, from its pointer attributes: 0 host memory,
+// 1 memory the current GPU's kernels may use directly (its own device memory,
+// or managed memory), -1 device memory of another GPU (kernels would read it
+// through peer access or fault, so it is refused).
+inline int classify_pointer(int type, int ptr_device, int current_device) {
+  if (type == cudaMemoryTypeManaged) return 1;
+  if (type != cudaMemoryTypeDevice) return 0;
+  return ptr_device == current_device ? 1 : -1;
+}
+
+// True for a device buffer of the current GPU, false for host memory; throws
+// for device memory of another GPU.
+inline bool device_pointer(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const int kind = classify_pointer(at.type, at.device, dev);
+  if (kind < 0)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] a buffer lives on GPU " + std::to_string(at.device) +
+                    ", not on the current GPU " + std::to_string(dev));
+  return kind == 1;
+}
+
 // Owning device allocation that only grows.
 template <class T> struct DeviceBuffer {
   T *ptr = nullptr;

@@ -57,15 +57,7 @@ constexpr int kEnsLimit = 200;       // lanczos::Solver::iterationHardLimit
 constexpr int kEstChunk = 4 * kEnsThreads;  // elements of one system per estimate CTA
 constexpr double kDummyFar = 1e5;    // dummy particles: radii away from everything
 
-bool ens_is_device_ptr(const void *p) {
-  if (!p) return false;
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
+bool ens_is_device_ptr(const void *p) { return device_pointer(p); }
 
 // ---------------------------------------------------------------------------
 // Kernels

@@ -366,7 +366,7 @@ inline int tridiag_sqrt_e1(const double *alpha, const double *beta, int m,
 // so that its spectrum is centred on 1; each node is one tridiagonal solve
 // (Thomas, stable for SPD), O(m), and the nodes are independent.  Node
 // spacing and range are chosen from the condition number so that the scalar
-// rule is within 1e-13 relative of 1/sqrt(lambda) over the whole spectrum
+// rule is within about 1e-13 relative of 1/sqrt(lambda) over the whole spectrum
 // (checked on a log grid; 54 to 134 nodes for kappa 1e2 to 1e8); the product
 // T (T^{-1/2} e1) adds rounding of order sqrt(kappa) eps.  Returns 0,
 // or 2 when T is not positive definite, kappa is above 1e8 or a bound fails:

@@ -15,8 +15,10 @@
 // sources of a target tile are split (a performance limit only); the particle
 // count itself is limited to kMaxParticles.
 //
-// Set-up: the first call on a device, with that device current, looks up the
-// device addresses of the arrays (cudaGetSymbolAddress) and caches them; make
+// Set-up: every call, with its device current, looks up the device addresses
+// of the arrays (cudaGetSymbolAddress: cheap, allocates nothing), so a device
+// reset or another context on the device never leaves a stale address; the
+// first call on a device also loads the library's device code there, so make
 // that first call before any stream capture.  Every call shares the arrays and
 // they keep the last call's contents: the tickets, which must start at zero,
 // are cleared by each call on its stream; two calls whose work overlaps on the
@@ -26,6 +28,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "common.hpp"
 #include "libmobility_gb300.h"
 #include "mdot_launch.cuh"
 #include "rpy_pair.cuh"
@@ -75,11 +78,11 @@ lmg_status setup(DeviceScratch *&out, char *err, size_t len) {
     return fail(err, len, LMG_ERR_INVALID_ARGUMENT, "[libmobility_gb300] device ordinal too large");
   std::lock_guard<std::mutex> lock(g_mutex);
   DeviceScratch &d = g_devices[dev];
+  e = cudaGetSymbolAddress((void **)&d.partials, g_noalloc_partials);
+  if (e != cudaSuccess) return fail_cuda(err, len, "cudaGetSymbolAddress(partials)", e);
+  e = cudaGetSymbolAddress((void **)&d.tickets, g_noalloc_tickets);
+  if (e != cudaSuccess) return fail_cuda(err, len, "cudaGetSymbolAddress(tickets)", e);
   if (!d.ready) {
-    e = cudaGetSymbolAddress((void **)&d.partials, g_noalloc_partials);
-    if (e != cudaSuccess) return fail_cuda(err, len, "cudaGetSymbolAddress(partials)", e);
-    e = cudaGetSymbolAddress((void **)&d.tickets, g_noalloc_tickets);
-    if (e != cudaSuccess) return fail_cuda(err, len, "cudaGetSymbolAddress(tickets)", e);
     e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return fail_cuda(err, len, "cudaDeviceGetAttribute", e);
     d.ready = true;
@@ -88,13 +91,20 @@ lmg_status setup(DeviceScratch *&out, char *err, size_t len) {
   return LMG_OK;
 }
 
-bool on_device(const void *p) {
+// 1: device memory of the current GPU (or managed), 0: host memory, -1:
+// device memory of another GPU.
+int on_device(const void *p) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return 0;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return lmg::classify_pointer(at.type, at.device, dev);
 }
 
 }  // namespace
@@ -131,11 +141,18 @@ extern "C" lmg_status lmg_mdot_noalloc_f32(const float *pos, const float *F, con
     return fail(err, err_len, LMG_ERR_INVALID_ARGUMENT,
                 "[libmobility_gb300] lmg_mdot_noalloc_f32 needs W when includeAngular is set");
   const void *bufs[5] = {pos, F, T, U, W};
-  for (const void *b : bufs)
-    if (b && !on_device(b))
+  for (const void *b : bufs) {
+    if (!b) continue;
+    const int kind = on_device(b);
+    if (kind < 0)
+      return fail(err, err_len, LMG_ERR_INVALID_ARGUMENT,
+                  "[libmobility_gb300] lmg_mdot_noalloc_f32: a buffer lives on another GPU "
+                  "than the current one");
+    if (kind == 0)
       return fail(err, err_len, LMG_ERR_INVALID_ARGUMENT,
                   "[libmobility_gb300] lmg_mdot_noalloc_f32 takes device buffers only (it "
                   "cannot stage host memory without allocating)");
+  }
 
   DeviceScratch *d = nullptr;
   lmg_status st = setup(d, err, err_len);

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "krylov.cuh"
+#include "common.hpp"
 #include "launch_count.hpp"
 #include "mdot_sym.cuh"
 
@@ -150,6 +151,13 @@ int lmg_internal_sym_plan(int N, int nper, long long resident, int force_warps, 
   if (warps) std::memcpy(warps, p.warps.data(), p.warps.size() * sizeof(int4));
   if (tused) std::memcpy(tused, p.tused.data(), p.tused.size() * sizeof(int));
   return 0;
+}
+
+// The decision behind every buffer check (0 host, 1 current GPU or managed,
+// -1 another GPU's memory) for given pointer attributes, so that it can be
+// checked without a second GPU.
+int lmg_internal_classify_pointer(int type, int ptr_device, int current_device) {
+  return lmg::classify_pointer(type, ptr_device, current_device);
 }
 
 // Timeline of the next symmetric-kernel launches (measurement hook, off when

@@ -28,16 +28,7 @@ namespace lmg {
 
 namespace {
 
-bool is_device_ptr(const void *p) {
-  if (!p) return false;
-  cudaPointerAttributes at;
-  cudaError_t e = cudaPointerGetAttributes(&at, p);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
+bool is_device_ptr(const void *p) { return device_pointer(p); }
 
 template <class R>
 __global__ void shift_min_kernel(R *pos, int N, R height, double *partials, unsigned *ticket,

@@ -262,3 +262,17 @@ def test_tridiagonal_quadrature_defers_to_exact_form(lib):
     out = np.zeros(40)
     assert lib.lmg_internal_tridiag_sqrt_e1_quad(a.ctypes.data, b.ctypes.data, 40,
                                                  out.ctypes.data) == 2
+
+
+def test_buffers_of_another_gpu_are_refused():
+    """The decision behind every buffer check, for given pointer attributes
+    (cudaMemoryType: 0 unregistered, 1 host, 2 device, 3 managed): device
+    memory of another GPU is refused (-1), never read on the host or through
+    peer access."""
+    from libmobility_gb300 import _capi
+    lib = _capi.load()
+    f = lib.lmg_internal_classify_pointer
+    assert f(0, -1, 0) == 0 and f(1, 0, 0) == 0      # host memory
+    assert f(2, 0, 0) == 1 and f(2, 3, 3) == 1       # this GPU's memory
+    assert f(2, 1, 0) == -1 and f(2, 0, 5) == -1     # another GPU's memory
+    assert f(3, 1, 0) == 1                           # managed memory

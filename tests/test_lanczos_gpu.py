@@ -221,3 +221,29 @@ def test_grid_barrier_wait_is_bounded(cuda):
     s.setPositions(np.random.default_rng(2).uniform(0, 10, (30, 3)))
     u, _ = s.sqrtMdotW()
     assert np.isfinite(u).all() and np.abs(u).max() > 0
+
+
+@pytest.mark.parametrize("precision", ["float", "double"])
+def test_nan_in_noise_reports_and_handle_stays_usable(cuda, precision):
+    """A NaN in the dW given to sqrtMdotW_noise (injected on the host) ends the
+    solve with the reference's error (LanczosAlgorithm.cu:210-213), and the
+    same handle then solves a clean dW exactly as a fresh handle does."""
+    rng = np.random.default_rng(321)
+    N = 200
+    p = rng.uniform(0, 20, (N, 3))
+    z = rng.normal(size=3 * N)
+    bad = z.copy()
+    bad[17] = np.nan
+
+    def fresh():
+        s = make_solver(0, 0, 1.0, 1 / (6 * np.pi), precision)
+        s.setPositions(p)
+        return s
+
+    s = fresh()
+    with pytest.raises(RuntimeError, match=r"found NaN in result guess"):
+        s.sqrtMdotW_noise(bad)
+    u, _, it, _ = s.sqrtMdotW_noise(z)
+    u2, _, it2, _ = fresh().sqrtMdotW_noise(z)
+    assert it == it2
+    assert np.array_equal(np.asarray(u), np.asarray(u2))

@@ -106,3 +106,50 @@ def test_noalloc_rejects_bad_arguments(cuda):
     assert rc == 1 and b"device buffers only" in err.value
     rc = lib.lmg_mdot_noalloc_f32(p, p, p, p, None, 4, -1, 0, 1.0, 1.0, 0, None, err, 256)
     assert rc == 1 and b"angular" in err.value
+
+
+@pytest.mark.parametrize("wall,ang,N", [(1, 1, 2048), (0, 0, 4096)])
+def test_noalloc_matches_fp64_oracle(cuda, oracle, wall, ang, N):
+    """Parity of the allocation-free entry point on its own, independent of the
+    handle API: two calls in a row against the FP64 oracle (1e-5 relative)."""
+    import torch
+    from libmobility_gb300 import _capi
+    lib = _capi.load()
+    rng = np.random.default_rng(900 + N)
+    if wall:
+        pos = np.column_stack([rng.uniform(0, 64, N), rng.uniform(0, 64, N),
+                               rng.uniform(0.5, 15, N)])
+    else:
+        pos = rng.uniform(0, (N * 4 * np.pi / 3 / 0.05) ** (1 / 3), (N, 3))
+    F = rng.normal(size=(N, 3))
+    T = rng.normal(size=(N, 3)) if ang else None
+    a, eta = 1.1, 0.7
+    Uo, Wo = oracle.mdot(pos, F, T, a=a, viscosity=eta, wall=wall, include_angular=ang)
+    f32 = dict(dtype=torch.float32, device="cuda")
+    dpos, dF = torch.tensor(pos, **f32), torch.tensor(F, **f32)
+    dT = torch.tensor(T, **f32) if ang else None
+    U = torch.empty((N, 3), **f32)
+    W = torch.empty((N, 3), **f32) if ang else None
+    err = ctypes.create_string_buffer(256)
+    ptr = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for call in range(2):
+        U.fill_(float("nan"))
+        rc = lib.lmg_mdot_noalloc_f32(ptr(dpos), ptr(dF), ptr(dT), ptr(U), ptr(W), N, -1, wall,
+                                      eta, a, ang, stream, err, 256)
+        assert rc == 0, err.value.decode()
+        torch.cuda.synchronize()
+        assert _rel(U.cpu().numpy(), Uo) <= 1e-5, call
+        if ang:
+            assert _rel(W.cpu().numpy(), Wo) <= 1e-5, call
+
+
+def test_noalloc_needs_forces_or_torques(cuda):
+    import torch
+    from libmobility_gb300 import _capi
+    lib = _capi.load()
+    err = ctypes.create_string_buffer(256)
+    d = torch.zeros((4, 3), device="cuda")
+    p = ctypes.c_void_p(d.data_ptr())
+    rc = lib.lmg_mdot_noalloc_f32(p, None, None, p, None, 4, -1, 0, 1.0, 1.0, 0, None, err, 256)
+    assert rc == 1 and b"F and/or T" in err.value
