@@ -112,6 +112,7 @@ def load():
         "lmg_internal_precond_apply": [_VP, _VP, _I, _VP, _VP, _I, _VP],
         "lmg_internal_knn_k": [_I, _VP, _I, _I, _VP, _VP],
         "lmg_internal_precond_build_kh": [_I, _I, _VP, _VP, _I, _VP, _F, _F, _VP, _VP],
+        "lmg_internal_precond_build_wall": [_I, _I, _VP, _VP, _I, _VP, _F, _F, _VP, _VP],
         "lmg_internal_precond_apply_k": [_I, _VP, _VP, _I, _VP, _VP, _I, _VP],
         "lmg_internal_precond_apply_kh": [_I, _VP, _I, _VP, _I, _VP, _VP, _I, _VP, _VP],
         "lmg_internal_lanczos_phase_timing": [_VP, _I],

@@ -292,11 +292,12 @@ cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaSt
 // ---------------------------------------------------------------------------
 constexpr int kBuildThreads = 128;
 
-template <int K>
+template <int K, bool WALL>
 __global__ void __launch_bounds__(kBuildThreads)
 precond_features_kernel(const float *__restrict__ pos, const int *__restrict__ nb, int N,
                         const float *__restrict__ xmean, const float *__restrict__ xstd,
                         float inv_a, float *__restrict__ X, float *__restrict__ E) {
+  constexpr int In = 3 * K + (WALL ? 1 : 0);
   const int i = blockIdx.x * kBuildThreads + threadIdx.x;
   if (i >= N) return;
   const int *nbi = nb + i;  // nb[n][i]
@@ -310,9 +311,27 @@ precond_features_kernel(const float *__restrict__ pos, const int *__restrict__ n
     rel[n][2] = (pos[3 * j + 2] - zi) * inv_a;
   }
   // canonical frame: x to the nearest neighbour, y to the first neighbour
-  // that is not collinear with it, z = x cross y
+  // that is not collinear with it, z = x cross y; with a wall, z is the wall
+  // normal and x the horizontal direction to the nearest neighbour that is
+  // not straight above or below
   float e[3][3];
-  {
+  if (WALL) {
+    float c = 1.f, s = 0.f;
+    bool found = false;
+#pragma unroll
+    for (int n = 0; n < K; n++) {
+      const float hh = rel[n][0] * rel[n][0] + rel[n][1] * rel[n][1];
+      if (!found && hh > 1e-12f) {
+        const float li = rsqrtf(hh);
+        c = rel[n][0] * li;
+        s = rel[n][1] * li;
+        found = true;
+      }
+    }
+    e[0][0] = c;   e[0][1] = s;   e[0][2] = 0.f;
+    e[1][0] = -s;  e[1][1] = c;   e[1][2] = 0.f;
+    e[2][0] = 0.f; e[2][1] = 0.f; e[2][2] = 1.f;
+  } else {
     const float l = rsqrtf(fmaxf(rel[0][0] * rel[0][0] + rel[0][1] * rel[0][1] +
                                  rel[0][2] * rel[0][2], 1e-30f));
     e[0][0] = rel[0][0] * l;
@@ -343,7 +362,7 @@ precond_features_kernel(const float *__restrict__ pos, const int *__restrict__ n
     e[2][1] = e[0][2] * y0 - e[0][0] * y2;
     e[2][2] = e[0][0] * y1 - e[0][1] * y0;
   }
-  float *x = X + (size_t)i * 3 * K;
+  float *x = X + (size_t)i * In;
 #pragma unroll
   for (int n = 0; n < K; n++) {
 #pragma unroll
@@ -351,6 +370,10 @@ precond_features_kernel(const float *__restrict__ pos, const int *__restrict__ n
       const float v = rel[n][0] * e[c][0] + rel[n][1] * e[c][1] + rel[n][2] * e[c][2];
       x[3 * n + c] = (v - xmean[3 * n + c]) / xstd[3 * n + c];
     }
+  }
+  if (WALL) {  // height above the wall, clamped at one radius as the physics does
+    const float h = fmaxf(zi * inv_a, 1.f);
+    x[3 * K] = (h - xmean[3 * K]) / xstd[3 * K];
   }
 #pragma unroll
   for (int r = 0; r < 3; r++)
@@ -427,10 +450,20 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
   const int g = (N + kBuildThreads - 1) / kBuildThreads;
   const float *xm = params + L.Xm, *xs = params + L.Xs;
   count_launch();
-  if (L.K == 16) precond_features_kernel<16><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
-  if (L.K == 32) precond_features_kernel<32><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
-  if (L.K == 48) precond_features_kernel<48><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
-  if (L.K == 64) precond_features_kernel<64><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, inv_a, X, E);
+#define LMG_FEATURES(KK)                                                                   \
+  if (L.K == KK) {                                                                         \
+    if (L.wall)                                                                            \
+      precond_features_kernel<KK, true><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, \
+                                                                         inv_a, X, E);     \
+    else                                                                                   \
+      precond_features_kernel<KK, false><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm,   \
+                                                                          xs, inv_a, X, E); \
+  }
+  LMG_FEATURES(16)
+  LMG_FEATURES(32)
+  LMG_FEATURES(48)
+  LMG_FEATURES(64)
+#undef LMG_FEATURES
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
     e = gemm_launch(0, 0, N, L.H, L.In, X, L.In, params + L.W1, L.H, H1, L.H, params + L.B1, 1,
@@ -842,6 +875,18 @@ int lmg_internal_precond_build_kh(int K, int H, const float *pos, const int *nb,
   }
 }
 
+
+// The same for a wall network (frame about the wall normal, height input).
+int lmg_internal_precond_build_wall(int K, int H, const float *pos, const int *nb, int N,
+                                    const float *params, float inv_a, float scale, float *blocks,
+                                    void *stream) {
+  try {
+    return (int)precond_build_launch(prec_layout(K, H, true), pos, nb, N, params, inv_a, scale,
+                                     blocks, false, nullptr, (cudaStream_t)stream);
+  } catch (const std::exception &) {
+    return (int)cudaErrorMemoryAllocation;
+  }
+}
 
 // Either product with float (half = 0) or half blocks (half = 1, applied
 // with scale 1).  The transposed product needs a float4 work array of N

@@ -14,7 +14,11 @@
 //   input   the K neighbours' positions relative to i, sorted by distance, in a
 //           canonical frame (x towards the nearest neighbour, y towards the
 //           next non-collinear one), divided by a and normalised  -> 3K values
-//   layers  3K -> 64 (tanh) -> 64 (tanh) -> 6 + 9K (linear)
+//   (wall networks, for a single bottom wall: the frame turns about the wall
+//   normal only -- x towards the horizontal offset of the nearest neighbour
+//   that has one, z the wall normal -- and the particle's height max(h, a)/a
+//   is one more input, 3K + 1 values)
+//   layers  3K (+1) -> H (tanh) -> H (tanh) -> 6 + 9K (linear)
 //   output  normalised entries of the self block (6, symmetric) and of the K
 //           neighbour blocks (9 each) in the canonical frame; rotated back to
 //           the lab frame and scaled by t0^{-1/2}.
@@ -30,21 +34,24 @@
 namespace lmg {
 
 // Network shape for K neighbours (16, 32, 48 or 64) and hidden width H (64, 128,
-// 256, 512 or 1024): parameters and normalisation, FP32, in one contiguous array:
-//   W1[3K][H] b1[H] W2[H][H] b2[H] W3[H][6+9K] b3[6+9K]
-//   xmean[3K] xstd[3K] ymean[6+9K] ystd[6+9K]
-// Every (K, H) pair has a different parameter count, which identifies it.
+// 256, 512 or 1024), In = 3K inputs (3K + 1 for a wall network): parameters
+// and normalisation, FP32, in one contiguous array:
+//   W1[In][H] b1[H] W2[H][H] b2[H] W3[H][6+9K] b3[6+9K]
+//   xmean[In] xstd[In] ymean[6+9K] ystd[6+9K]
+// Every (K, H, wall) has a different parameter count, which identifies it.
 struct PrecLayout {
   int K = 0, H = 0, In = 0, Out = 0;
+  bool wall = false;  // trained on a bottom wall: frame about z, height input
   int W1 = 0, B1 = 0, W2 = 0, B2 = 0, W3 = 0, B3 = 0, Xm = 0, Xs = 0, Ym = 0, Ys = 0;
   int Params = 0;
 };
 
-inline PrecLayout prec_layout(int K, int H) {
+inline PrecLayout prec_layout(int K, int H, bool wall = false) {
   PrecLayout L;
   L.K = K;
   L.H = H;
-  L.In = 3 * K;
+  L.wall = wall;
+  L.In = 3 * K + (wall ? 1 : 0);
   L.Out = 6 + 9 * K;
   L.W1 = 0;
   L.B1 = L.W1 + L.In * H;
@@ -62,11 +69,12 @@ inline PrecLayout prec_layout(int K, int H) {
 
 // The layout whose parameter count is n (K = 0 if there is none).
 inline PrecLayout prec_layout_for_params(size_t n) {
-  for (int K : {16, 32, 48, 64})
-    for (int H : {64, 128, 256, 512, 1024}) {
-      const PrecLayout L = prec_layout(K, H);
-      if ((size_t)L.Params == n) return L;
-    }
+  for (bool wall : {false, true})
+    for (int K : {16, 32, 48, 64})
+      for (int H : {64, 128, 256, 512, 1024}) {
+        const PrecLayout L = prec_layout(K, H, wall);
+        if ((size_t)L.Params == n) return L;
+      }
   return PrecLayout{};
 }
 

@@ -865,7 +865,11 @@ void Solver<R>::set_preconditioner(const std::string &kind, const float *params,
     throw Error(LMG_ERR_INVALID_ARGUMENT,
                 "[libmobility_gb300] preconditioner parameters: " + std::to_string(n) +
                     " floats is not the size of a network over K = 16, 32, 48 or 64 neighbours "
-                    "with 64, 128, 256 or 512 hidden units");
+                    "with 64, 128, 256, 512 or 1024 hidden units");
+  if (L.wall && !wall_)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] this preconditioner network was trained above a wall; "
+                "the solver has an open boundary");
   float *d = prec_params_.ensure(n);
   LMG_CUDA(cudaMemcpy(d, params, n * sizeof(float), cudaMemcpyHostToDevice));
   prec_layout_ = L;

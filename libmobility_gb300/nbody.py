@@ -156,7 +156,9 @@ class NBody:
     def setPreconditioner(self, kind="mlp", weights=None):
         """Learned sparse preconditioner for sqrtMdotW (no counterpart in
         the reference): "mlp" uses the network shipped in
-        libmobility_gb300/weights (or the .npz given as `weights`); "none"
+        libmobility_gb300/weights for the handle's geometry (the wall network
+        for a single wall when one is shipped), or the .npz given as
+        `weights`; "none"
         restores plain Lanczos.  The statistics of the samples do not depend
         on it, only the number of Lanczos iterations."""
         if kind == "none":
@@ -164,8 +166,8 @@ class NBody:
             return
         from . import precond
         params = np.ascontiguousarray(
-            precond.load_weights(weights) if not isinstance(weights, np.ndarray) else weights,
-            dtype=np.float32)
+            precond.load_weights(weights, wall=self._wall)
+            if not isinstance(weights, np.ndarray) else weights, dtype=np.float32)
         self._prec_params = params
         self._check(self._lib.lmg_set_preconditioner(self._h, str(kind).encode(),
                                                      ctypes.c_void_p(params.ctypes.data),

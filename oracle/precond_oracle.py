@@ -11,10 +11,10 @@ K = 16
 NH = 64
 
 
-def shapes(k=K, h=NH):
+def shapes(k=K, h=NH, wall=False):
     """Parameter layout of the network for k neighbours and h hidden units
-    (3k -> h -> h -> 6 + 9k)."""
-    nin, nout = 3 * k, 6 + 9 * k
+    (3k -> h -> h -> 6 + 9k; one more input, the height, above a wall)."""
+    nin, nout = 3 * k + (1 if wall else 0), 6 + 9 * k
     return [("W1", (nin, h)), ("b1", (h,)), ("W2", (h, h)), ("b2", (h,)),
             ("W3", (h, nout)), ("b3", (nout,)), ("xmean", (nin,)), ("xstd", (nin,)),
             ("ymean", (nout,)), ("ystd", (nout,))]
@@ -24,13 +24,19 @@ SHAPES = shapes(K)
 NIN, NOUT = 3 * K, 6 + 9 * K
 
 
+def khw_of(flat):
+    """(neighbours, hidden units, wall) of a flat parameter vector."""
+    for wall in (False, True):
+        for k in (16, 32, 48, 64):
+            for h in (64, 128, 256, 512, 1024):
+                if len(flat) == sum(int(np.prod(s)) for _, s in shapes(k, h, wall)):
+                    return k, h, wall
+    raise ValueError("not a preconditioner parameter vector")
+
+
 def kh_of(flat):
     """(neighbours, hidden units) of a flat parameter vector."""
-    for k in (16, 32, 48, 64):
-        for h in (64, 128, 256, 512, 1024):
-            if len(flat) == sum(int(np.prod(s)) for _, s in shapes(k, h)):
-                return k, h
-    raise ValueError("not a preconditioner parameter vector")
+    return khw_of(flat)[:2]
 
 
 def k_of(flat):
@@ -39,7 +45,7 @@ def k_of(flat):
 
 def unpack(flat):
     out, o = {}, 0
-    for k, shp in shapes(*kh_of(flat)):
+    for k, shp in shapes(*khw_of(flat)):
         n = int(np.prod(shp))
         out[k] = np.asarray(flat[o:o + n], np.float64).reshape(shp)
         o += n
@@ -68,6 +74,19 @@ def frame(rel):
     return np.stack([x, y, np.cross(x, y)])
 
 
+def wall_frame(rel):
+    """Rows: x to the horizontal offset of the first neighbour that has one,
+    y = z cross x, z the wall normal."""
+    for r in rel:
+        hh = r[0] ** 2 + r[1] ** 2
+        if hh > 1e-12:
+            c, s_ = r[0] / np.sqrt(hh), r[1] / np.sqrt(hh)
+            break
+    else:
+        c, s_ = 1.0, 0.0
+    return np.array([[c, s_, 0.0], [-s_, c, 0.0], [0.0, 0.0, 1.0]])
+
+
 def forward(d, X):
     """Returns (H1, H2, Ynorm) for normalised inputs X (B, 48)."""
     H1 = np.tanh(X @ d["W1"] + d["b1"])
@@ -88,16 +107,21 @@ def backward(d, X, H1, H2, Y, T):
 
 
 def p_blocks(pos, flat, a=1.0, scale=1.0):
-    """Lab-frame blocks (N, K+1, 3, 3) and neighbour lists (N, K+1)."""
+    """Lab-frame blocks (N, K+1, 3, 3) and neighbour lists (N, K+1); a wall
+    network (3K + 1 inputs) takes its frame about the wall normal and the
+    height max(z, a)/a as its last input."""
     d = unpack(flat)
-    K = k_of(flat)
+    K, _, wall = khw_of(flat)
     nb, _ = neighbours(pos, K)
     N = pos.shape[0]
     out = np.zeros((N, K + 1, 3, 3))
     for i in range(N):
         rel = (pos[nb[i, 1:]] - pos[i]) / a
-        E = frame(rel)
-        x = ((rel @ E.T).ravel() - d["xmean"]) / d["xstd"]
+        E = wall_frame(rel) if wall else frame(rel)
+        feat = (rel @ E.T).ravel()
+        if wall:
+            feat = np.append(feat, max(pos[i, 2] / a, 1.0))
+        x = (feat - d["xmean"]) / d["xstd"]
         _, _, y = forward(d, x[None, :])
         y = y[0] * d["ystd"] + d["ymean"]
         b = [np.array([[y[0], y[1], y[2]], [y[1], y[3], y[4]], [y[2], y[4], y[5]]])]

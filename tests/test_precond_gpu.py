@@ -155,6 +155,45 @@ def test_wider_networks_match_oracle(cuda, po, K, H):
         assert np.allclose(out.cpu().numpy(), ref_y, rtol=1e-4, atol=1e-5 * np.abs(ref_y).max())
 
 
+@pytest.mark.parametrize("K,H", [(16, 64), (48, 128)])
+def test_wall_network_build_matches_oracle(cuda, po, K, H):
+    """The wall network's features (frame about the wall normal, height input,
+    clamped at one radius) and P blocks against the NumPy oracle, on a slab
+    above the wall with heights from below the radius up."""
+    import torch
+    lib = _lib()
+    rng = np.random.default_rng(70 + K)
+    N = 240
+    p = np.column_stack([rng.uniform(0, 30, N), rng.uniform(0, 30, N),
+                         rng.uniform(0.4, 12, N)]).astype(np.float32)
+    d = {k: rng.normal(0, 0.3, shp) for k, shp in po.shapes(K, H, True)}
+    d["xstd"] = np.abs(d["xstd"]) + 1.0
+    d["ystd"] = np.abs(d["ystd"]) + 0.5
+    params = np.concatenate([np.asarray(d[k], np.float32).ravel()
+                             for k, _ in po.shapes(K, H, True)])
+    dp = torch.tensor(p, device="cuda")
+    nb = torch.empty((K + 1, N), dtype=torch.int32, device="cuda")
+    blocks = torch.empty((K + 1, 9, N), dtype=torch.float32, device="cuda")
+    dparams = torch.tensor(params, device="cuda")
+    assert lib.lmg_internal_knn_k(K, ctypes.c_void_p(dp.data_ptr()), N, N,
+                                  ctypes.c_void_p(nb.data_ptr()), None) == 0
+    a, scale = 1.2, 0.9
+    assert lib.lmg_internal_precond_build_wall(K, H, ctypes.c_void_p(dp.data_ptr()),
+                                              ctypes.c_void_p(nb.data_ptr()), N,
+                                              ctypes.c_void_p(dparams.data_ptr()), 1.0 / a,
+                                              scale, ctypes.c_void_p(blocks.data_ptr()),
+                                              None) == 0
+    torch.cuda.synchronize()
+    ref, nb_ref = po.p_blocks(p.astype(np.float64), params, a=a, scale=scale)
+    got = blocks.cpu().numpy().transpose(2, 0, 1).reshape(N, K + 1, 3, 3)
+    nbg = nb.cpu().numpy().T
+    for i in range(N):
+        assert set(nbg[i]) == set(nb_ref[i])
+        m = {int(j): got[i, n] for n, j in enumerate(nbg[i])}
+        for n, j in enumerate(nb_ref[i]):
+            assert np.allclose(m[int(j)], ref[i, n], rtol=2e-3, atol=2e-4 * np.abs(ref[i]).max())
+
+
 @pytest.mark.parametrize("K", [16, 48, 64])
 def test_half_block_products_match_dense(cuda, po, K):
     """P x and P^T x with half-precision blocks (the solver's storage), the
