@@ -622,6 +622,42 @@ def large_wall_mdot(torch, rank, reps=3):
             "achieved_tflops": pairs * FLOPS_PER_PAIR[("wall", True)] / t / 1e12}
 
 
+def large_wall_sqrt(torch, rank):
+    """Configuration 5's square root: single wall, N = 262144, x, y ~ U[0,
+    1024), z ~ U[1.5, 40], includeAngular, FP32, tolerance 1e-6: one
+    sqrtMdotW of plain Lanczos and one with the learned wall preconditioner
+    (rebuilt for the solve), same dW, wall time and iterations."""
+    from libmobility_gb300 import NBody
+    N = 262144
+    rng = np.random.default_rng(31 + rank)
+    pos = np.column_stack([rng.uniform(0, 1024, N), rng.uniform(0, 1024, N),
+                           rng.uniform(1.5, 40, N)])
+    dpos = torch.tensor(pos, dtype=torch.float32, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(13 + rank)
+    dW = torch.randn(6 * N, generator=g, device="cuda")
+    out = {"workload": "single wall, N=262144, x,y ~ U[0,1024), z ~ U[1.5,40], includeAngular, "
+                       "FP32, tolerance 1e-6, one solve per arm (same dW)"}
+    for kind in ("none", "mlp"):
+        s = NBody("open", "open", "single_wall", precision="float")
+        s.setParameters(wallHeight=0.0)
+        s.initialize(viscosity=1 / (6 * math.pi), hydrodynamicRadius=1.0, includeAngular=True,
+                     tolerance=1e-6, seed=3 + rank)
+        s.setPreconditioner(kind)
+        s.setPositions(dpos)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.setPositions(dpos)
+        _, _, it, res = s.sqrtMdotW_noise(dW)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        out[kind] = {"ms_per_solve": t * 1e3, "lanczos_iterations": it, "residual": res}
+        if kind == "mlp":
+            out[kind]["network"] = "wall, 48 neighbours, 512-512 hidden"
+            out[kind]["p_solve_iterations"] = s.lastPreconditionerSolveIterations()
+    out["speedup_learned_vs_plain"] = out["none"]["ms_per_solve"] / out["mlp"]["ms_per_solve"]
+    return out
+
+
 def hbm_peak_gbs():
     """The measured copy bandwidth (GB/s), None when the file is absent."""
     try:
@@ -847,10 +883,11 @@ def run_ours(args, w, ws, rank, local):
     ens = None
     if not args.skip_ensemble:
         ens = ensemble_comparison(torch, max(2, args.steps), 2, rank)
-    large = None
+    large = large_sqrt = None
     if not args.skip_large:
         large = large_wall_mdot(torch, rank)
         large["frac_of_fp32_peak"] = large["achieved_tflops"] / peak
+        large_sqrt = large_wall_sqrt(torch, rank)
 
     if rank != 0:
         return
@@ -873,6 +910,7 @@ def run_ours(args, w, ws, rank, local):
         "sqrtMdotW_learned_vs_plain": cmp,
         "ensemble_256": ens,
         "wall_262k_mdot": large,
+        "wall_262k_sqrt": large_sqrt,
         "open4k_mdot": open4k,
         "reference_gpu": ref_gpu,
         "krylov_phases": krylov,
@@ -909,10 +947,10 @@ def main():
     ap.add_argument("--skip-ensemble", action="store_true",
                     help="skip the batched ensemble of 256 uneven systems")
     ap.add_argument("--skip-large", action="store_true",
-                    help="skip the N = 262144 single-wall Mdot")
+                    help="skip the N = 262144 single-wall Mdot and square roots")
     ap.add_argument("--skip-reference-gpu", action="store_true",
                     help="skip the reference CUDA kernel timed beside this library's Mdot")
-    ap.add_argument("--only", choices=["ensemble", "precond", "open4k"], default=None,
+    ap.add_argument("--only", choices=["ensemble", "precond", "open4k", "large"], default=None,
                     help="run one sub-measurement alone and print it (for profiling)")
     ap.add_argument("--ensemble-systems", type=int, default=256)
     args = ap.parse_args()
@@ -930,6 +968,12 @@ def main():
         out = sqrtmdotw_comparison(torch, args.steps, args.warmup, rank)
         if rank == 0:
             print(json.dumps({"sqrtMdotW_learned_vs_plain": out}))
+        return
+    if args.only == "large":  # configuration 5's square roots alone
+        import torch
+        out = large_wall_sqrt(torch, rank)
+        if rank == 0:
+            print(json.dumps({"wall_262k_sqrt": out}))
         return
     if args.only == "open4k":  # configuration 1 alone (profiling runs)
         import torch
