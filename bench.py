@@ -321,6 +321,46 @@ def open4k_mdot(torch, lib, peak32, peak64, flush):
     return out, pos, F, results
 
 
+def open4k_sqrt(torch, lib, solves=20):
+    """Configuration 1's square root: open boundary, N = 4096, FP32,
+    tolerance 1e-6, sqrtMdotW solves per second (host wall clock around each
+    call, device-resident dW) with T^{1/2} e1 of the convergence checks on the
+    device (quadrature, the default) and on the host (exact QL), on fresh
+    handles after 3 warm-up solves each."""
+    from libmobility_gb300 import NBody
+    pos, _ = config1_inputs()
+    N = pos.shape[0]
+    dpos = torch.tensor(pos, dtype=torch.float32, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(17)
+    dWs = [torch.randn(3 * N, generator=g, device="cuda") for _ in range(solves + 3)]
+    out = {"workload": "open RPY, N=4096, cube at phi=0.05, FP32, tolerance 1e-6"}
+    try:
+        for name, dev in (("device_sqrt", 1), ("host_sqrt", 0)):
+            assert lib.lmg_internal_lanczos_device_sqrt(dev) == 0
+            s = NBody("open", "open", "open", precision="float")
+            s.setParameters()
+            s.initialize(viscosity=1 / (6 * math.pi), hydrodynamicRadius=1.0, tolerance=1e-6,
+                         seed=9)
+            s.setPositions(dpos)
+            its, ts = [], []
+            for k, dW in enumerate(dWs):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                _, _, it, _ = s.sqrtMdotW_noise(dW)
+                torch.cuda.synchronize()
+                if k >= 3:
+                    ts.append(time.perf_counter() - t0)
+                    its.append(it)
+            t = sum(ts) / len(ts)
+            out[name] = {"solves_per_s": 1.0 / t, "ms_per_solve": t * 1e3,
+                         "lanczos_iterations": sum(its) / len(its)}
+    finally:
+        lib.lmg_internal_lanczos_device_sqrt(1)
+    out["speedup_device_vs_host_sqrt"] = (out["device_sqrt"]["solves_per_s"]
+                                          / out["host_sqrt"]["solves_per_s"])
+    return out
+
+
 def reference_gpu_mdot(torch, wall16k_inputs):
     """libMobility's own NBody CUDA kernel (computeRPYBatchedFastGPU, launch
     shape of its launcher, NbodyRPY.cu:99-116), compiled for sm_103a from the
@@ -836,6 +876,7 @@ def run_ours(args, w, ws, rank, local):
     peak = fp32_peak_tflops(lib, torch)
     peak64 = fp64_peak_tflops(lib, torch)
     open4k, pos1, F1, res1 = open4k_mdot(torch, lib, peak, peak64, flush)
+    open4k_sq = open4k_sqrt(torch, lib)
     ref_gpu = None
     if not args.skip_reference_gpu:
         ref_gpu = reference_gpu_mdot(torch, (pos, F, T, dW))
@@ -912,6 +953,7 @@ def run_ours(args, w, ws, rank, local):
         "wall_262k_mdot": large,
         "wall_262k_sqrt": large_sqrt,
         "open4k_mdot": open4k,
+        "open4k_sqrt": open4k_sq,
         "reference_gpu": ref_gpu,
         "krylov_phases": krylov,
         "mdot_pair_interactions_per_s": pairs / t_mdot,
@@ -982,8 +1024,9 @@ def main():
         flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
         out, _, _, _ = open4k_mdot(torch, lib, fp32_peak_tflops(lib, torch),
                                    fp64_peak_tflops(lib, torch), flush)
+        sq = open4k_sqrt(torch, lib)
         if rank == 0:
-            print(json.dumps({"open4k_mdot": out}))
+            print(json.dumps({"open4k_mdot": out, "open4k_sqrt": sq}))
         return
     if args.impl == "reference":
         run_reference(args, w, ws, rank)

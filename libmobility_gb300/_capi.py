@@ -121,6 +121,7 @@ def load():
         "lmg_internal_sym_override": [_I, _I],
         "lmg_internal_sym_trace": [_VP],
         "lmg_internal_classify_pointer": [_I, _I, _I],
+        "lmg_internal_lanczos_device_sqrt": [_I],
     }
     for name, args in internal.items():
         fn = getattr(lib, name)

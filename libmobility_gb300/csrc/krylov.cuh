@@ -476,6 +476,154 @@ inline int tridiag_sqrt_e1_quad(const double *alpha, const double *beta, int m, 
 }
 
 // y = |z| V_m c   (V row-major: row k is v_k, n elements)
+// ---------------------------------------------------------------------------
+// T^{1/2} e1 on the device, by the quadrature of tridiag_sqrt_e1_quad (same
+// spectrum bounds, node rule, weights and node order), so that a convergence
+// check needs no host eigen-solve and no copy of its coefficients.  One block:
+// the positive-definiteness test and the 4^-j lower-bound candidates are one
+// Sturm count per thread; then thread q sweeps quadrature node q (forward
+// elimination and back substitution of (T/s + t_q^2 I) g = e1, FP64) and
+// writes w_q g to scratch; the node sums are folded in node order and T is
+// applied.  *flag (mapped host memory) becomes 0, or 1 when T is not
+// positive definite or its condition number exceeds 1e8: then `out` is not
+// written and the caller takes the exact eigen-solution on the host.
+// ---------------------------------------------------------------------------
+constexpr int kQuadThreads = 256;  // >= the largest node count (135) and m
+
+__device__ __forceinline__ int sturm_count_below(const double *a, const double *b, int m,
+                                                 double x) {
+  int c = 0;
+  double d = 1.0;
+  for (int k = 0; k < m; k++) {
+    const double bb = k > 0 ? b[k - 1] * b[k - 1] : 0.0;
+    d = (a[k] - x) - (k > 0 ? bb / d : 0.0);
+    if (d == 0.0) d = -1e-300;  // x is an eigenvalue: count it as below
+    if (d < 0.0) c++;
+  }
+  return c;
+}
+
+static __global__ void __launch_bounds__(kQuadThreads)
+tridiag_sqrt_quad_kernel(const KrylovScalars *sc, int m, double *out, double *G,
+                         double *flag) {
+  __shared__ double a[kQuadThreads], b[kQuadThreads], acc[kQuadThreads];
+  __shared__ int cnt[15];
+  __shared__ double s_hi, s_lo;
+  __shared__ int s_state;  // 0 go on, 1 fall back
+  const int t = threadIdx.x;
+  for (int k = t; k < m; k += kQuadThreads) {
+    a[k] = sc->alpha[k];
+    b[k] = sc->beta[k];
+  }
+  __syncthreads();
+  if (m == 1) {
+    if (t == 0) {
+      if (a[0] > 0.0) {
+        out[0] = sqrt(a[0]);
+        *flag = 0.0;
+      } else {
+        *flag = 1.0;
+      }
+    }
+    return;
+  }
+  if (t == 0) {  // upper bound of the spectrum (Gershgorin)
+    double hi = 0.0;
+    for (int k = 0; k < m; k++) {
+      const double r = (k > 0 ? fabs(b[k - 1]) : 0.0) + (k + 1 < m ? fabs(b[k]) : 0.0);
+      hi = fmax(hi, a[k] + r);
+    }
+    s_hi = hi;
+    s_state = (hi > 0.0 && isfinite(hi)) ? 0 : 1;
+  }
+  __syncthreads();
+  if (s_state) {
+    if (t == 0) *flag = 1.0;
+    return;
+  }
+  // thread 0: eigenvalues below 0; thread j = 1..14: below hi * 4^-(j-1)
+  if (t < 15) cnt[t] = sturm_count_below(a, b, m, t == 0 ? 0.0 : ldexp(s_hi, -2 * (t - 1)));
+  __syncthreads();
+  if (t == 0) {
+    int state = cnt[0] > 0 ? 1 : 0;
+    double lo = 0.0;
+    if (!state) {
+      int j = 0;
+      while (j < 14 && cnt[j + 1] > 0) j++;
+      if (j == 14) state = 1;  // below hi * 1e-8
+      else lo = ldexp(s_hi, -2 * j);
+    }
+    s_lo = lo;
+    s_state = state;
+  }
+  __syncthreads();
+  if (s_state) {
+    if (t == 0) *flag = 1.0;
+    return;
+  }
+  const double hi = s_hi, lo = s_lo;
+  const double kappa = hi / lo;
+  double h, vmax;
+  if (kappa <= 1e2) {
+    h = 0.15;
+    vmax = 4.0;
+  } else if (kappa <= 1e4) {
+    h = 0.1;
+    vmax = 4.0;
+  } else if (kappa <= 1e6) {
+    h = 0.08;
+    vmax = 4.5;
+  } else {
+    h = 0.06;
+    vmax = 4.0;
+  }
+  const double sq = sqrt(lo * hi), is = 1.0 / sq;
+  const int half = (int)(vmax / h + 0.5);
+  const int nodes = 2 * half + 1;
+  if (t < nodes) {
+    constexpr double kPi = 3.14159265358979323846;
+    const double v = (t - half) * h;
+    const double tt = exp(0.5 * kPi * sinh(v));
+    const double t2 = tt * tt;
+    const double w = h * cosh(v) * tt;
+    double *g = G + (size_t)t * 2 * kQuadThreads;  // gp[m], then cp[m]
+    double *cp = g + kQuadThreads;
+    {
+      const double inv = 1.0 / (a[0] * is + t2);
+      cp[0] = b[0] * is * inv;
+      g[0] = inv;
+    }
+    for (int k = 1; k < m; k++) {
+      const double ek = b[k - 1] * is;
+      const double bk = k + 1 < m ? b[k] * is : 0.0;
+      const double inv = 1.0 / (a[k] * is + t2 - ek * cp[k - 1]);
+      cp[k] = bk * inv;
+      g[k] = -ek * g[k - 1] * inv;
+    }
+    double x = g[m - 1];
+    g[m - 1] = w * x;
+    for (int k = m - 2; k >= 0; k--) {
+      x = g[k] - cp[k] * x;
+      g[k] = w * x;
+    }
+  }
+  __syncthreads();
+  for (int k = t; k < m; k += kQuadThreads) {  // node order, as the host sums
+    double s = 0.0;
+    for (int q = 0; q < nodes; q++) s += G[(size_t)q * 2 * kQuadThreads + k];
+    acc[k] = s;
+  }
+  __syncthreads();
+  const double f = 1.0 / sqrt(sq);
+  for (int k = t; k < m; k += kQuadThreads) {
+    double y = a[k] * acc[k];
+    if (k > 0) y += b[k - 1] * acc[k - 1];
+    if (k + 1 < m) y += b[k] * acc[k + 1];
+    out[k] = f * y;
+  }
+  if (t == 0) *flag = 0.0;
+}
+
 template <class R>
 __global__ void krylov_estimate_kernel(const R *V, size_t ldv, int m, const double *c,
                                        const KrylovScalars *sc, R *y, size_t n) {

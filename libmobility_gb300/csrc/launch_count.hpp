@@ -13,6 +13,9 @@ extern std::atomic<int> g_force_tpt, g_force_split;
 // g_sym_warps > 0 caps the warps its steps are spread over; g_sym_variant is
 // its register budget, 2, 3 or 4 resident blocks per SM (0 = default, 2)
 extern std::atomic<int> g_sym_mode, g_sym_warps, g_sym_variant;
+// T^{1/2} e1 of the single-system Lanczos checks: 1 (default) on the device by
+// quadrature, the exact host QL where it falls back; 0 always the host QL
+extern std::atomic<int> g_lanczos_device_sqrt;
 // device buffer for the symmetric kernel's timeline (null = off)
 extern std::atomic<unsigned long long *> g_sym_trace;
 }  // namespace lmg

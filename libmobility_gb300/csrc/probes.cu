@@ -22,6 +22,7 @@ std::atomic<unsigned long long> g_launches{0};
 std::atomic<int> g_force_tpt{0}, g_force_split{0};
 std::atomic<int> g_sym_mode{0}, g_sym_warps{0}, g_sym_variant{0};
 std::atomic<unsigned long long *> g_sym_trace{nullptr};
+std::atomic<int> g_lanczos_device_sqrt{1};
 }
 
 namespace {
@@ -150,6 +151,16 @@ int lmg_internal_sym_plan(int N, int nper, long long resident, int force_warps, 
   if (pseg) std::memcpy(pseg, p.pseg.data(), p.pseg.size() * sizeof(int));
   if (warps) std::memcpy(warps, p.warps.data(), p.warps.size() * sizeof(int4));
   if (tused) std::memcpy(tused, p.tused.data(), p.tused.size() * sizeof(int));
+  return 0;
+}
+
+// Where the single-system Lanczos takes T^{1/2} e1 at its checks: 1 (the
+// default) on the device by quadrature, with the exact host QL where the
+// quadrature does not apply; 0 always the host QL.  Applies to the next
+// solves of every handle.
+int lmg_internal_lanczos_device_sqrt(int on) {
+  if (on != 0 && on != 1) return 1;
+  lmg::g_lanczos_device_sqrt.store(on);
   return 0;
 }
 

@@ -127,6 +127,7 @@ template <class R> class Solver final : public SolverBase {
   DeviceBuffer<double> cvec_;
   MappedBuffer<double> mirror_;       // (alpha_i, beta_i) pairs + err, device-written
   PinnedBuffer<double> hc_;           // T^{1/2} e1 staged for the device (2 slots)
+  DeviceBuffer<double> quad_g_;       // node sums of the device square root
   std::vector<double> ql_work_;       // host QL work arrays
   std::vector<double2> rot_cs_;       // host QL rotation log
   std::vector<int> rot_idx_;
@@ -208,7 +209,7 @@ template <class R> void Solver<R>::release_all() {
   pos_.release(); pos_tmp_.release(); in_stage_.release(); out_stage_.release(); pin_.release();
   part_.release(); tickets_.release(); red_part_.release(); red_ticket_.release(); dmin_.release();
   V_.release(); w_.release(); y_.release(); ybuf_.release(); z_.release(); sc_.release();
-  cvec_.release(); mirror_.release(); hc_.release(); ql_work_ = {}; rot_cs_ = {}; rot_idx_ = {};
+  cvec_.release(); mirror_.release(); hc_.release(); quad_g_.release(); ql_work_ = {}; rot_cs_ = {}; rot_idx_ = {};
   h_dbl_.release(); rfd_noise_.release(); rfd_pos_.release(); rfd_mp_.release(); rfd_mm_.release();
   plans_.clear();
   sym_plans_.clear();
@@ -495,9 +496,12 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
   R *yb = ybuf_.ensure(2 * n);
   KrylovScalars *sc = sc_.ensure(1);
   double *cdev = cvec_.ensure(2 * kMaxLanczosIterations);
-  double *mir = mirror_.ensure(2 * 256 + 8);  // [2i] alpha_i, [2i+1] beta_i, [512] err
+  // [2i] alpha_i, [2i+1] beta_i, [512] err, [516] barrier timeout, [520]
+  // device square root fell back
+  double *mir = mirror_.ensure(2 * 256 + 16);
   double *mir_dev = mirror_.device_ptr();
   double *hc = hc_.ensure(2 * kMaxLanczosIterations);
+  double *quad_g = quad_g_.ensure((size_t)kQuadThreads * 2 * kQuadThreads);
   const int rot_cap = 24 * limit * limit + 1024;
   if ((int)rot_cs_.size() < rot_cap) {
     rot_cs_.resize(rot_cap);
@@ -563,37 +567,55 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     if (i + 1 < limit) issue(i + 1);
     if (!(i >= k || cb_ != nullptr)) continue;
     const int m = i + 1;
-    LMG_CUDA(cudaEventSynchronize(ev_iter_[i & 1]));
-    if (mir[516] != 0.0)
-      throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
-    for (int q = 0; q < m; q++) {
-      al[q] = mir[2 * q];
-      be[q] = mir[2 * q + 1];
-    }
-    double *c = hc + (i & 1) * kMaxLanczosIterations;
-    const int rc = tridiag_sqrt_e1(al.data(), be.data(), m, ql_work_.data(),
-                                   ql_work_.data() + 256, ql_work_.data() + 512, log, c);
-    if (rc != 0)
-      for (int q = 0; q < m; q++) c[q] = std::nan("");
     double *cd = cdev + (i & 1) * kMaxLanczosIterations;
     R *yi = yb + (size_t)(i & 1) * n;
-    LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i & 1], 0));
-    if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
-    LMG_CUDA(cudaMemcpyAsync(cd, c, m * sizeof(double), cudaMemcpyHostToDevice, sd));
-    krylov_estimate_kernel<R><<<blocks, kRedThreads, 0, sd>>>(V, n, m, cd, sc, yi, n);
-    count_launch();
-    if (have_prev) {
-      krylov_error_kernel<R><<<blocks, kRedThreads, 0, sd>>>(
-          yi, yb + (size_t)((i + 1) & 1) * n, n, rp_side, tk_side, sc, mir_dev + 512);
+    // estimate y = |z| V c and its error against the previous estimate, on
+    // the side stream once c is in device memory
+    auto estimate_and_error = [&]() {
+      krylov_estimate_kernel<R><<<blocks, kRedThreads, 0, sd>>>(V, n, m, cd, sc, yi, n);
       count_launch();
+      if (have_prev) {
+        krylov_error_kernel<R><<<blocks, kRedThreads, 0, sd>>>(
+            yi, yb + (size_t)((i + 1) & 1) * n, n, rp_side, tk_side, sc, mir_dev + 512);
+        count_launch();
+      }
+      if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 4], sd));
+      LMG_CUDA(cudaEventRecord(ev_check_, sd));
+      LMG_CUDA(cudaGetLastError());
+      LMG_CUDA(cudaEventSynchronize(ev_check_));
+    };
+    bool on_host = g_lanczos_device_sqrt.load() == 0;
+    if (!on_host) {
+      // c = T^{1/2} e1 by quadrature on the device, right after iteration i
+      LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i & 1], 0));
+      if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
+      tridiag_sqrt_quad_kernel<<<1, kQuadThreads, 0, sd>>>(sc, m, cd, quad_g, mir_dev + 520);
+      count_launch();
+      estimate_and_error();
+      if (mir[516] != 0.0)
+        throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
+      on_host = mir[520] != 0.0;  // not positive definite or too ill-conditioned
     }
-    if (timing_) {
-      LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 4], sd));
-      checked.push_back(i);
+    if (on_host) {
+      // the exact eigen-solution of T on the host (implicit QL, FP64)
+      LMG_CUDA(cudaEventSynchronize(ev_iter_[i & 1]));
+      if (mir[516] != 0.0)
+        throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
+      for (int q = 0; q < m; q++) {
+        al[q] = mir[2 * q];
+        be[q] = mir[2 * q + 1];
+      }
+      double *c = hc + (i & 1) * kMaxLanczosIterations;
+      const int rc = tridiag_sqrt_e1(al.data(), be.data(), m, ql_work_.data(),
+                                     ql_work_.data() + 256, ql_work_.data() + 512, log, c);
+      if (rc != 0)
+        for (int q = 0; q < m; q++) c[q] = std::nan("");
+      LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i & 1], 0));
+      if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
+      LMG_CUDA(cudaMemcpyAsync(cd, c, m * sizeof(double), cudaMemcpyHostToDevice, sd));
+      estimate_and_error();
     }
-    LMG_CUDA(cudaEventRecord(ev_check_, sd));
-    LMG_CUDA(cudaGetLastError());
-    LMG_CUDA(cudaEventSynchronize(ev_check_));
+    if (timing_) checked.push_back(i);
     err = have_prev ? mir[512] : HUGE_VAL;
     if (have_prev) {  // the reference never tests the first estimate (i > 0 there)
       if (residual) *residual = err;

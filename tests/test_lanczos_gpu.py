@@ -247,3 +247,33 @@ def test_nan_in_noise_reports_and_handle_stays_usable(cuda, precision):
     u2, _, it2, _ = fresh().sqrtMdotW_noise(z)
     assert it == it2
     assert np.array_equal(np.asarray(u), np.asarray(u2))
+
+
+@pytest.mark.parametrize("precision", ["float", "double"])
+@pytest.mark.parametrize("wall", [0, 1])
+def test_device_and_host_square_roots_agree(cuda, precision, wall):
+    """T^{1/2} e1 at the convergence checks by quadrature on the device (the
+    default) or by the exact QL on the host: the same stopping step and the
+    same result (FP64 within 1e-12, FP32 within 1e-6), on fresh handles."""
+    from libmobility_gb300 import _capi
+    lib = _capi.load()
+    rng = np.random.default_rng(90 + wall)
+    N = 300
+    p = rng.uniform(0, 25, (N, 3))
+    if wall:
+        p[:, 2] = rng.uniform(1.2, 10, N)
+    zs = [rng.normal(size=3 * N) for _ in range(3)]
+    out = {}
+    try:
+        for dev in (1, 0):
+            assert lib.lmg_internal_lanczos_device_sqrt(dev) == 0
+            s = make_solver(wall, 0, 1.0, 1 / (6 * np.pi), precision)
+            s.setPositions(p)
+            out[dev] = [s.sqrtMdotW_noise(z) for z in zs]
+    finally:
+        lib.lmg_internal_lanczos_device_sqrt(1)
+    tol = 1e-12 if precision == "double" else 1e-6
+    for (u1, _, it1, _), (u0, _, it0, _) in zip(out[1], out[0]):
+        assert it1 == it0
+        u1, u0 = np.asarray(u1, np.float64), np.asarray(u0, np.float64)
+        assert np.abs(u1 - u0).max() <= tol * np.abs(u0).max()
