@@ -122,6 +122,7 @@ def load():
         "lmg_internal_sym_trace": [_VP],
         "lmg_internal_classify_pointer": [_I, _I, _I],
         "lmg_internal_lanczos_device_sqrt": [_I],
+        "lmg_internal_lanczos_lookahead": [_I],
     }
     for name, args in internal.items():
         fn = getattr(lib, name)

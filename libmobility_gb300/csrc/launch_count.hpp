@@ -16,6 +16,8 @@ extern std::atomic<int> g_sym_mode, g_sym_warps, g_sym_variant;
 // T^{1/2} e1 of the single-system Lanczos checks: 1 (default) on the device by
 // quadrature, the exact host QL where it falls back; 0 always the host QL
 extern std::atomic<int> g_lanczos_device_sqrt;
+// iterations issued ahead of a check (0 = by batch size: 3 up to 8192 particles, else 1)
+extern std::atomic<int> g_lanczos_lookahead;
 // device buffer for the symmetric kernel's timeline (null = off)
 extern std::atomic<unsigned long long *> g_sym_trace;
 }  // namespace lmg

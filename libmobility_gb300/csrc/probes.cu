@@ -23,6 +23,7 @@ std::atomic<int> g_force_tpt{0}, g_force_split{0};
 std::atomic<int> g_sym_mode{0}, g_sym_warps{0}, g_sym_variant{0};
 std::atomic<unsigned long long *> g_sym_trace{nullptr};
 std::atomic<int> g_lanczos_device_sqrt{1};
+std::atomic<int> g_lanczos_lookahead{0};
 }
 
 namespace {
@@ -161,6 +162,15 @@ int lmg_internal_sym_plan(int N, int nper, long long resident, int force_warps, 
 int lmg_internal_lanczos_device_sqrt(int on) {
   if (on != 0 && on != 1) return 1;
   lmg::g_lanczos_device_sqrt.store(on);
+  return 0;
+}
+
+// Iterations the single-system Lanczos issues ahead of the check it is
+// evaluating: 1..4, or 0 for the default (3 for batches of up to 8192
+// particles, else 1).
+int lmg_internal_lanczos_lookahead(int n) {
+  if (n < 0 || n > 4) return 1;
+  lmg::g_lanczos_lookahead.store(n);
   return 0;
 }
 

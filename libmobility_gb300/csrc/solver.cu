@@ -133,7 +133,10 @@ template <class R> class Solver final : public SolverBase {
   std::vector<int> rot_idx_;
   PinnedBuffer<double> h_dbl_;
   cudaStream_t side_ = nullptr;       // high-priority stream for per-check work
-  cudaEvent_t ev_iter_[2] = {nullptr, nullptr}, ev_check_ = nullptr, ev_side_ = nullptr;
+  // iteration j completes ev_iter_[j % kIterEvents] (a ring: up to kMaxLookahead
+  // iterations run ahead of the check being evaluated)
+  static constexpr int kMaxLookahead = 4, kIterEvents = kMaxLookahead + 2;
+  cudaEvent_t ev_iter_[kIterEvents] = {}, ev_check_ = nullptr, ev_side_ = nullptr;
   // phase timing: per iteration j, [5j, 5j+1] bracket the operator, [5j+1,
   // 5j+2] the vector updates and [5j+3, 5j+4] the check; ev_pre_ the
   // preconditioner build and P solve (created on the first timed solve)
@@ -538,6 +541,13 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
   if (timing_) ensure_phase_events();
   int issued = 0;
   std::vector<int> checked;
+  auto nper_lookahead = [&]() {
+    const int forced = g_lanczos_lookahead.load();
+    if (forced > 0) return std::min(forced, (int)kMaxLookahead);
+    // one matrix-vector product of a batch of up to 8192 particles takes
+    // tens of microseconds, less than a check
+    return batch_size() <= 8192 ? 3 : 1;
+  };
   auto issue = [&](int j) {
     R *vj = V + (size_t)j * n;
     if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * j], st));
@@ -553,7 +563,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
                                          dim3(kRedThreads), args, 0, st));
     count_launch();
     if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * j + 2], st));
-    LMG_CUDA(cudaEventRecord(ev_iter_[j & 1], st));
+    LMG_CUDA(cudaEventRecord(ev_iter_[j % kIterEvents], st));
     issued = j + 1;
   };
 
@@ -563,8 +573,13 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
   bool have_prev = false;
   int done = -1;
   double err = 0;
+  // iterations issued ahead of the check of iteration i: the check (a host or
+  // device square root of T, the estimate and its error) waits for the
+  // host, so with cheap matrix-vector products several iterations keep the
+  // GPU busy meanwhile; past convergence they are discarded
+  int ahead = nper_lookahead();
   for (int i = 0; i < limit; i++) {
-    if (i + 1 < limit) issue(i + 1);
+    while (issued <= i + ahead && issued < limit) issue(issued);
     if (!(i >= k || cb_ != nullptr)) continue;
     const int m = i + 1;
     double *cd = cdev + (i & 1) * kMaxLanczosIterations;
@@ -587,7 +602,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     bool on_host = g_lanczos_device_sqrt.load() == 0;
     if (!on_host) {
       // c = T^{1/2} e1 by quadrature on the device, right after iteration i
-      LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i & 1], 0));
+      LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i % kIterEvents], 0));
       if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
       tridiag_sqrt_quad_kernel<<<1, kQuadThreads, 0, sd>>>(sc, m, cd, quad_g, mir_dev + 520);
       count_launch();
@@ -598,7 +613,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     }
     if (on_host) {
       // the exact eigen-solution of T on the host (implicit QL, FP64)
-      LMG_CUDA(cudaEventSynchronize(ev_iter_[i & 1]));
+      LMG_CUDA(cudaEventSynchronize(ev_iter_[i % kIterEvents]));
       if (mir[516] != 0.0)
         throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
       for (int q = 0; q < m; q++) {
@@ -610,7 +625,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
                                      ql_work_.data() + 256, ql_work_.data() + 512, log, c);
       if (rc != 0)
         for (int q = 0; q < m; q++) c[q] = std::nan("");
-      LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i & 1], 0));
+      LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i % kIterEvents], 0));
       if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
       LMG_CUDA(cudaMemcpyAsync(cd, c, m * sizeof(double), cudaMemcpyHostToDevice, sd));
       estimate_and_error();
