@@ -325,7 +325,7 @@ def open4k_sqrt(torch, lib, solves=20):
     """Configuration 1's square root: open boundary, N = 4096, FP32,
     tolerance 1e-6, sqrtMdotW solves per second (host wall clock around each
     call, device-resident dW) with T^{1/2} e1 of the convergence checks on the
-    device (quadrature, the default) and on the host (exact QL), on fresh
+    host (exact QL, the default) and on the device (quadrature), on fresh
     handles after 3 warm-up solves each."""
     from libmobility_gb300 import NBody
     pos, _ = config1_inputs()
@@ -355,7 +355,7 @@ def open4k_sqrt(torch, lib, solves=20):
             out[name] = {"solves_per_s": 1.0 / t, "ms_per_solve": t * 1e3,
                          "lanczos_iterations": sum(its) / len(its)}
     finally:
-        lib.lmg_internal_lanczos_device_sqrt(1)
+        lib.lmg_internal_lanczos_device_sqrt(0)
     out["speedup_device_vs_host_sqrt"] = (out["device_sqrt"]["solves_per_s"]
                                           / out["host_sqrt"]["solves_per_s"])
     return out

@@ -479,7 +479,9 @@ inline int tridiag_sqrt_e1_quad(const double *alpha, const double *beta, int m, 
 // ---------------------------------------------------------------------------
 // T^{1/2} e1 on the device, by the quadrature of tridiag_sqrt_e1_quad (same
 // spectrum bounds, node rule, weights and node order), so that a convergence
-// check needs no host eigen-solve and no copy of its coefficients.  One block:
+// check needs no host eigen-solve and no copy of its coefficients (an
+// option: with GB300's narrow FP64 units this chain of FP64 divisions takes
+// longer than the host's QL at the sizes measured, ~40 us a check).  One block:
 // the positive-definiteness test and the 4^-j lower-bound candidates are one
 // Sturm count per thread; then thread q sweeps quadrature node q (forward
 // elimination and back substitution of (T/s + t_q^2 I) g = e1, FP64) and

@@ -13,8 +13,8 @@ extern std::atomic<int> g_force_tpt, g_force_split;
 // g_sym_warps > 0 caps the warps its steps are spread over; g_sym_variant is
 // its register budget, 2, 3 or 4 resident blocks per SM (0 = default, 2)
 extern std::atomic<int> g_sym_mode, g_sym_warps, g_sym_variant;
-// T^{1/2} e1 of the single-system Lanczos checks: 1 (default) on the device by
-// quadrature, the exact host QL where it falls back; 0 always the host QL
+// T^{1/2} e1 of the single-system Lanczos checks: 0 (default) the exact host
+// QL; 1 on the device by quadrature, the host QL where that falls back
 extern std::atomic<int> g_lanczos_device_sqrt;
 // iterations issued ahead of a check (0 = by batch size: 3 up to 8192 particles, else 1)
 extern std::atomic<int> g_lanczos_lookahead;

@@ -22,7 +22,7 @@ std::atomic<unsigned long long> g_launches{0};
 std::atomic<int> g_force_tpt{0}, g_force_split{0};
 std::atomic<int> g_sym_mode{0}, g_sym_warps{0}, g_sym_variant{0};
 std::atomic<unsigned long long *> g_sym_trace{nullptr};
-std::atomic<int> g_lanczos_device_sqrt{1};
+std::atomic<int> g_lanczos_device_sqrt{0};
 std::atomic<int> g_lanczos_lookahead{0};
 }
 
@@ -155,10 +155,13 @@ int lmg_internal_sym_plan(int N, int nper, long long resident, int force_warps, 
   return 0;
 }
 
-// Where the single-system Lanczos takes T^{1/2} e1 at its checks: 1 (the
-// default) on the device by quadrature, with the exact host QL where the
-// quadrature does not apply; 0 always the host QL.  Applies to the next
-// solves of every handle.
+// Where the single-system Lanczos takes T^{1/2} e1 at its checks: 0 (the
+// default) the exact QL on the host; 1 on the device by quadrature, with the
+// host QL where the quadrature does not apply.  Applies to the next solves
+// of every handle.  (Measured at N = 4096: 6.0 ms per solve on the host, 8.4
+// ms on the device: the quadrature is a chain of FP64 divisions, and its
+// kernels cannot overlap the cooperative matrix-vector and vector-step
+// launches, so every check's device time adds to the solve.)
 int lmg_internal_lanczos_device_sqrt(int on) {
   if (on != 0 && on != 1) return 1;
   lmg::g_lanczos_device_sqrt.store(on);

@@ -252,8 +252,8 @@ def test_nan_in_noise_reports_and_handle_stays_usable(cuda, precision):
 @pytest.mark.parametrize("precision", ["float", "double"])
 @pytest.mark.parametrize("wall", [0, 1])
 def test_device_and_host_square_roots_agree(cuda, precision, wall):
-    """T^{1/2} e1 at the convergence checks by quadrature on the device (the
-    default) or by the exact QL on the host: the same stopping step and the
+    """T^{1/2} e1 at the convergence checks by the exact QL on the host (the
+    default) or by quadrature on the device: the same stopping step and the
     same result (FP64 within 1e-12, FP32 within 1e-6), on fresh handles."""
     from libmobility_gb300 import _capi
     lib = _capi.load()
@@ -271,7 +271,7 @@ def test_device_and_host_square_roots_agree(cuda, precision, wall):
             s.setPositions(p)
             out[dev] = [s.sqrtMdotW_noise(z) for z in zs]
     finally:
-        lib.lmg_internal_lanczos_device_sqrt(1)
+        lib.lmg_internal_lanczos_device_sqrt(0)
     tol = 1e-12 if precision == "double" else 1e-6
     for (u1, _, it1, _), (u0, _, it0, _) in zip(out[1], out[0]):
         assert it1 == it0
