@@ -1,6 +1,7 @@
 // Shared host-side definitions: status-carrying exception and CUDA checks.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstring>
 #include <stdexcept>
@@ -62,6 +63,15 @@ inline bool device_pointer(const void *p) {
                     ", not on the current GPU " + std::to_string(dev));
   return kind == 1;
 }
+
+// Named range on the profiler timeline (NVTX) for the lifetime of the object:
+// the entry points and the phases of a solve (a no-op without a profiler).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Owning device allocation that only grows.
 template <class T> struct DeviceBuffer {

@@ -844,6 +844,7 @@ template <class R> void Ensemble<R>::build_graph(R *V, size_t ldv) {
 }
 
 template <class R> void Ensemble<R>::mdot(const void *F, size_t nF, void *U, size_t nU) {
+  NvtxRange nvtx_range_("lmg ensemble Mdot");
   require_ready();
   const size_t n3 = 3 * (size_t)ntot_;
   if (!F || nF != n3 || !U || nU != n3)
@@ -875,6 +876,7 @@ template <class R> void Ensemble<R>::mdot(const void *F, size_t nF, void *U, siz
 template <class R>
 void Ensemble<R>::sqrt_mdot_w(const void *dW, size_t ndW, void *U, size_t nU, double pf,
                               int *its, double *errs, double *ms_out) {
+  NvtxRange nvtx_range_("lmg ensemble sqrtMdotW");
   if (pf == 0) return;  // MobilityInterface.h:150
   require_ready();
   const size_t n3 = 3 * (size_t)ntot_;

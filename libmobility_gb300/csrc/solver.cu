@@ -232,6 +232,7 @@ template <class R> void Solver<R>::ensure_reduction(int blocks) {
 }
 
 template <class R> void Solver<R>::set_positions(const void *pos, size_t n) {
+  NvtxRange nvtx_range_("lmg setPositions");
   if (n % 3 != 0)
     throw Error(LMG_ERR_INVALID_ARGUMENT,
                 "[libMobility] The input arrays for positions, forces, and torques must each "
@@ -426,6 +427,7 @@ template <class R> bool Solver<R>::mdot_sym(const R *pos, const R *F, R *U) {
 template <class R>
 void Solver<R>::mdot(const void *F, size_t nF, const void *T, size_t nT, void *U, size_t nU,
                      void *W, size_t nW) {
+  NvtxRange nvtx_range_("lmg Mdot");
   if (!F) nF = 0;
   if (!T) nT = 0;
   if (!U) nU = 0;
@@ -490,6 +492,7 @@ template <class R> void Solver<R>::ensure_phase_events() {
 
 template <class R>
 int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *residual) {
+  NvtxRange nvtx_range_("lmg Lanczos");
   const int limit = hard_limit_;
   const int blocks = vec_blocks(n);
   ensure_reduction(blocks);
@@ -599,6 +602,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
       LMG_CUDA(cudaGetLastError());
       LMG_CUDA(cudaEventSynchronize(ev_check_));
     };
+    NvtxRange nvtx_check("lmg Lanczos check");
     bool on_host = g_lanczos_device_sqrt.load() == 0;
     if (!on_host) {
       // c = T^{1/2} e1 by quadrature on the device, right after iteration i
@@ -686,6 +690,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
 template <class R>
 void Solver<R>::sqrt_mdot_w(void *U, size_t nU, void *W, size_t nW, double prefactor,
                             const void *dW, size_t ndW, int *iterations, double *residual) {
+  NvtxRange nvtx_range_("lmg sqrtMdotW");
   if (prefactor == 0) return;
   if (!initialized_)
     throw Error(LMG_ERR_NOT_INITIALIZED,
@@ -805,6 +810,7 @@ void Solver<R>::sqrt_mdot_w(void *U, size_t nU, void *W, size_t nW, double prefa
 // exactly as they were.
 template <class R>
 void Solver<R>::div_m(void *U, size_t nU, void *W, size_t nW, double prefactor) {
+  NvtxRange nvtx_range_("lmg divM");
   if (prefactor == 0) return;
   if (!wall_) return;  // no wall, no thermal drift (mobility.h:189-190)
   if (!U) nU = 0;
@@ -922,6 +928,7 @@ template <class R> bool Solver<R>::prec_active() const {
 }
 
 template <class R> void Solver<R>::prec_build() {
+  NvtxRange nvtx_range_("lmg preconditioner build");
   if constexpr (std::is_same<R, float>::value) {
     if (!prec_dirty_) return;
     const int N = (int)N_;
@@ -970,6 +977,7 @@ template <class R> void Solver<R>::apply_operator(const R *v, R *out) {
 // precision vectors).  Scalars in FP64 on the host; each reduction is read
 // back through mapped memory.
 template <class R> int Solver<R>::solve_p(const R *b, R *x) {
+  NvtxRange nvtx_range_("lmg preconditioner solve");
   if constexpr (!std::is_same<R, float>::value) {
     (void)b; (void)x;
     return 0;
