@@ -44,9 +44,9 @@ def _headers():
     return list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.hpp")) + list((ROOT / "include").glob("*.h"))
 
 
-def _compile(src, defs, obj):
+def _compile(src, defs, obj, objdir=None):
     s = CSRC / src
-    o = OBJ / obj
+    o = (objdir or OBJ) / obj
     deps = [s] + _headers()
     if o.exists() and all(d.stat().st_mtime <= o.stat().st_mtime for d in deps):
         return None
@@ -63,27 +63,34 @@ def _compile(src, defs, obj):
     return None
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile and link the library if any source is newer than it."""
-    OBJ.mkdir(exist_ok=True)
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
+    """Compile and link the library if any source is newer than it.  checked
+    = True makes the bounds-checked variant (-DLMG_BOUNDS_CHECK: failed index
+    checks record a status word and skip the access) as
+    liblmg_gb300_checked.so, from objects of its own."""
+    objdir = OBJ.parent / "_build_checked" if checked else OBJ
+    lib = LIB.with_name("liblmg_gb300_checked.so") if checked else LIB
+    extra = ["-DLMG_BOUNDS_CHECK"] if checked else []
+    objdir.mkdir(exist_ok=True)
     if force:
-        for p in OBJ.glob("*.o"):
+        for p in objdir.glob("*.o"):
             p.unlink()
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        errs = [e for e in ex.map(lambda u: _compile(*u), UNITS) if e]
+        errs = [e for e in ex.map(lambda u: _compile(u[0], u[1] + extra, u[2], objdir), UNITS)
+                if e]
     if errs:
         raise RuntimeError("libmobility_gb300 build failed:\n" + "\n".join(errs))
-    objs = [OBJ / u[2] for u in UNITS]
-    if force or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
-        cmd = [_nvcc(), "-shared", *ARCH, "-cudart", "static", "-o", str(LIB),
+    objs = [objdir / u[2] for u in UNITS]
+    if force or not lib.exists() or any(o.stat().st_mtime > lib.stat().st_mtime for o in objs):
+        cmd = [_nvcc(), "-shared", *ARCH, "-cudart", "static", "-o", str(lib),
                *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("libmobility_gb300 link failed:\n" + r.stdout + r.stderr)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib}")
+    return lib
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
+    build(force="--force" in sys.argv, verbose=True, checked="--checked" in sys.argv)

@@ -96,6 +96,10 @@ def load():
     lib.lmg_internal_fma_probe.argtypes = [_I, _I, _I, _VP, _VP]
     lib.lmg_internal_fma2_probe.restype = _I
     lib.lmg_internal_fma2_probe.argtypes = [_I, _I, _I, _VP, _VP]
+    lib.lmg_internal_bounds_status.restype = ctypes.c_ulonglong
+    lib.lmg_internal_bounds_status.argtypes = [_I, _I]
+    lib.lmg_internal_bounds_probe.restype = _I
+    lib.lmg_internal_bounds_probe.argtypes = []
     lib.lmg_internal_dfma_probe.restype = _I
     lib.lmg_internal_dfma_probe.argtypes = [_I, _I, _I, _VP, _VP]
     lib.lmg_internal_sym_plan.restype = _I

@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "bounds.cuh"
 #include "pack2.cuh"
 #include "rpy_pair.cuh"
 
@@ -51,6 +52,7 @@ template <class R> struct MdotArgs {
   WallConst kw;          // fused all-blocks wall constants (FP32 path)
   R *part;               // scratch: [tiles][nsplit][2*NC][BT]
   unsigned *ticket;      // scratch: [tiles]
+  size_t part_cap, ticket_cap;  // their sizes (index checks of the checked build)
   // optional per-batch flags (nsys entries, with sys_begin): a tile whose
   // batches are all flagged 0 is skipped by every one of its CTAs (outputs
   // left as they were, scratch and ticket untouched)
@@ -272,7 +274,7 @@ mdot_kernel(const MdotArgs<R> a) {
     {  // stage one tile of sources
       const int j = ts + threadIdx.x;
       Q4<R> p = {0, 0, 0, 0}, fv = {0, 0, 0, 0}, tv = {0, 0, 0, 0};
-      if (j < c_end) {
+      if (j < c_end && LMG_IN_BOUNDS(j < N, 1, j)) {
         R x = a.pos[3 * j], y = a.pos[3 * j + 1], z = a.pos[3 * j + 2];
         R b = R(1);
         p.x = mul_rn(x, ia);
@@ -510,7 +512,7 @@ mdot_kernel(const MdotArgs<R> a) {
     for (int t = 0; t < TPT; t++) {
       const int i = tgt0 + threadIdx.x + t * THREADS;
       if (i >= N) continue;
-      if (a.U) {
+      if (a.U && LMG_IN_BOUNDS(i < N, 5, i)) {
         a.U[3 * i] = bi[t] * (S[t][0] + C[t][0]);
         a.U[3 * i + 1] = bi[t] * (S[t][1] + C[t][1]);
         a.U[3 * i + 2] = bi[t] * (S[t][2] + C[t][2]);
@@ -525,20 +527,25 @@ mdot_kernel(const MdotArgs<R> a) {
   }
 
   // ---- split sources: publish partials, last CTA of the tile reduces ----
-  R *mine = a.part + ((size_t)(tile * nsplit + split) * (2 * NC)) * BT;
+  const size_t mine_off = ((size_t)(tile * nsplit + split) * (2 * NC)) * BT;
+  R *mine = a.part + mine_off;
 #pragma unroll
   for (int t = 0; t < TPT; t++) {
     const int l = threadIdx.x + t * THREADS;
 #pragma unroll
     for (int c = 0; c < NC; c++) {
-      __stcg(mine + (size_t)c * BT + l, S[t][c]);
-      __stcg(mine + (size_t)(NC + c) * BT + l, C[t][c]);
+      if (LMG_IN_BOUNDS(mine_off + (size_t)(NC + c) * BT + l < a.part_cap, 2,
+                        mine_off + (size_t)(NC + c) * BT + l)) {
+        __stcg(mine + (size_t)c * BT + l, S[t][c]);
+        __stcg(mine + (size_t)(NC + c) * BT + l, C[t][c]);
+      }
     }
   }
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned prev = atomicAdd(a.ticket + tile, 1u);
+    const unsigned prev = LMG_IN_BOUNDS((size_t)tile < a.ticket_cap, 4, tile)
+                              ? atomicAdd(a.ticket + tile, 1u) : 0u;
     s_last = (prev == (unsigned)(nsplit - 1));
   }
   __syncthreads();
@@ -560,7 +567,9 @@ mdot_kernel(const MdotArgs<R> a) {
 #pragma unroll
       for (int u = 0; u < UNR; u++) {
         // past the last split: re-read the last one (a valid address), add 0
-        const bool in = s0 + u < nsplit;
+        const bool in = s0 + u < nsplit &&
+                        LMG_IN_BOUNDS(((size_t)tile * nsplit + s0 + u + 1) * (2 * NC) * BT <=
+                                          a.part_cap, 3, tile);
         const R *ps = base + (size_t)(in ? s0 + u : nsplit - 1) * (2 * NC) * BT;
 #pragma unroll
         for (int c = 0; c < NC; c++) {
@@ -580,7 +589,7 @@ mdot_kernel(const MdotArgs<R> a) {
       }
     }
     if (i < N) {
-      if (a.U) {
+      if (a.U && LMG_IN_BOUNDS(i < N, 5, i)) {
         a.U[3 * i] = bi[t] * (Ss[0] + Cs[0]);
         a.U[3 * i + 1] = bi[t] * (Ss[1] + Cs[1]);
         a.U[3 * i + 2] = bi[t] * (Ss[2] + Cs[2]);

@@ -87,11 +87,18 @@ cudaError_t mdot_launch(const MdotShape &s, const MdotArgs<R> &args, const MdotP
   if (!k) return cudaErrorInvalidValue;
   MdotArgs<R> a = args;
   a.chunk = plan.chunk;
+  a.part_cap = plan.part_elems;
+  a.ticket_cap = plan.tickets;
   dim3 grid(plan.tiles, plan.nsplit);
   void *params[] = {(void *)&a};
   count_launch();
   return cudaLaunchKernel(k, grid, dim3(plan.threads), params, 0, stream);
 }
+
+// this translation unit's bounds status (the checked build; 0 otherwise)
+#define LMG_STATUS_FN(tag) bounds_status_mdot_##tag
+#define LMG_STATUS_NAME(tag) LMG_STATUS_FN(tag)
+unsigned long long LMG_STATUS_NAME(LMG_REAL)(bool reset) { return bounds_status_here(reset); }
 
 template cudaError_t mdot_plan<LMG_REAL>(const MdotShape &, int, int, int, int, int, MdotPlan &);
 template cudaError_t mdot_launch<LMG_REAL>(const MdotShape &, const MdotArgs<LMG_REAL> &,

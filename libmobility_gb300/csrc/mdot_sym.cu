@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "bounds.cuh"
 #include "grid_sync.cuh"
 #include "launch_count.hpp"
 #include "mdot.cuh"
@@ -26,7 +27,8 @@ struct SymArgs {
   const float *pos;
   const float *F;
   float *U;
-  int nper, tpb, ntiles, nwarps, lg_rt, cmax;
+  int N, nper, tpb, ntiles, nwarps, lg_rt, cmax;
+  size_t part_elems;  // floats of part (index checks of the checked build)
   float inv_a;
   // far-field coefficients in both lanes, f = ir (tf0 + tf1 ir^2),
   // G = ir^3 (tg0 + tg1 ir^2), prefactor t0 folded in
@@ -117,7 +119,7 @@ __device__ __forceinline__ int2 tile_desc(const SymArgs &a, int t) {
 
 __device__ __forceinline__ void load_slot(const SymArgs &a, int2 td, int lane, Slot &s) {
   const int p0 = 4 * lane;
-  if (p0 + 3 < td.y) {
+  if (p0 + 3 < td.y && LMG_IN_BOUNDS((size_t)td.x + p0 + 3 < (size_t)a.N, 11, td.x + p0)) {
     // 12 consecutive floats of positions and of forces (16-byte aligned)
     const float4 *P = reinterpret_cast<const float4 *>(a.pos + 3 * ((size_t)td.x + p0));
     const float4 *Fv = reinterpret_cast<const float4 *>(a.F + 3 * ((size_t)td.x + p0));
@@ -140,7 +142,8 @@ __device__ __forceinline__ void load_slot(const SymArgs &a, int2 td, int lane, S
   } else {
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      if (p0 + q < td.y) {
+      if (p0 + q < td.y && LMG_IN_BOUNDS((size_t)td.x + p0 + q < (size_t)a.N, 11,
+                                          td.x + p0 + q)) {
         const size_t g = 3 * ((size_t)td.x + p0 + q);
         s.x[q] = __fmul_rn(__ldg(a.pos + g), a.inv_a);
         s.y[q] = __fmul_rn(__ldg(a.pos + g + 1), a.inv_a);
@@ -403,13 +406,17 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
       }
       float vj[12] = {AX.x, AY.x, AZ.x, AX.y, AY.y, AZ.y,
                       AX.z, AY.z, AZ.z, AX.w, AY.w, AZ.w};
+      const size_t si = (size_t)(pr.z + seg) * kElems, sj = (size_t)(pr.w + seg) * kElems;
       if (diag) {
 #pragma unroll
         for (int c = 0; c < 12; c++) vi[c] += vj[c];
-        store12(a.part + (size_t)(pr.z + seg) * kElems + 12 * lane, vi);
+        if (LMG_IN_BOUNDS(si + kElems <= a.part_elems, 12, pr.z + seg))
+          store12(a.part + si + 12 * lane, vi);
       } else {
-        store12(a.part + (size_t)(pr.z + seg) * kElems + 12 * lane, vi);
-        store12(a.part + (size_t)(pr.w + seg) * kElems + 12 * lane, vj);
+        if (LMG_IN_BOUNDS(si + kElems <= a.part_elems, 12, pr.z + seg))
+          store12(a.part + si + 12 * lane, vi);
+        if (LMG_IN_BOUNDS(sj + kElems <= a.part_elems, 12, pr.w + seg))
+          store12(a.part + sj + 12 * lane, vj);
       }
       // the staged tile and the sums are overwritten by the next pair
       __syncwarp();
@@ -458,7 +465,10 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
 #pragma unroll
         for (int m = 0; m < 16; m++) {
           const int j = m0 + sub[h] + m * rt;
-          v[h][m] = j < cnt[h] ? __ldcg(src[h] + (size_t)j * kElems) : 0.f;
+          v[h][m] = (j < cnt[h] &&
+                     LMG_IN_BOUNDS(((size_t)t[h] * a.cmax + j + 1) * kElems <= a.part_elems, 13,
+                                   t[h]))
+                        ? __ldcg(src[h] + (size_t)j * kElems) : 0.f;
         }
 #pragma unroll
       for (int h = 0; h < 2; h++)
@@ -479,7 +489,8 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
       }
       if (in[h] && sub[h] == 0) {
         const int2 td = tile_desc(a, t[h]);
-        if (e[h] < 3 * td.y) a.U[3 * (size_t)td.x + e[h]] = S[h] + C[h];
+        if (e[h] < 3 * td.y && LMG_IN_BOUNDS(3 * (size_t)td.x + e[h] < 3 * (size_t)a.N, 14, td.x))
+          a.U[3 * (size_t)td.x + e[h]] = S[h] + C[h];
       }
     }
   }
@@ -501,6 +512,8 @@ const void *sym_kernel(int variant) {
 }
 
 }  // namespace
+
+unsigned long long bounds_status_sym(bool reset) { return bounds_status_here(reset); }
 
 cudaError_t mdot_sym_plan(int N, int nper, int num_sms, int force_warps, SymPlan &p) {
   const int v = g_sym_variant.load();
@@ -626,9 +639,11 @@ cudaError_t mdot_sym_launch(const SymPlan &p, const SymTables &tab, const float 
   a.pos = pos;
   a.F = F;
   a.U = U;
+  a.N = p.N;
   a.nper = p.nper;
   a.tpb = p.tpb;
   a.ntiles = p.nbatch * p.tpb;
+  a.part_elems = p.part_elems;
   a.nwarps = p.nwarps;
   a.cmax = p.cmax;
   int lg = 0;

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "krylov.cuh"
+#include "bounds.cuh"
 #include "common.hpp"
 #include "launch_count.hpp"
 #include "mdot_sym.cuh"
@@ -84,6 +85,13 @@ __global__ void dfma_chain_kernel(int iters, double *sink) {
 #pragma unroll
   for (int k = 0; k < 8; k++) s += a[k];
   if (s == -1.0) sink[threadIdx.x] = s;
+}
+
+// A check whose condition is false, on an index it never uses: in the
+// checked build it records code 99 (nothing is accessed).
+__global__ void bounds_probe_kernel(int limit) {
+  const int idx = limit + (int)threadIdx.x;
+  if (LMG_IN_BOUNDS(idx < limit, 99, idx)) asm volatile("" ::"r"(idx));
 }
 
 // Two blocks meet at a barrier whose arrival count starts at 7: neither is
@@ -182,6 +190,28 @@ int lmg_internal_lanczos_lookahead(int n) {
 // checked without a second GPU.
 int lmg_internal_classify_pointer(int type, int ptr_device, int current_device) {
   return lmg::classify_pointer(type, ptr_device, current_device);
+}
+
+// Status words of the checked build (compiled with -DLMG_BOUNDS_CHECK; 0 in
+// the normal build): the first failed index check of the all-pairs kernels
+// (FP32 and FP64) and of the symmetric kernel, as (code << 48) | index;
+// reset clears them.
+unsigned long long lmg_internal_bounds_status(int which, int reset) {
+  switch (which) {
+    case 0: return lmg::bounds_status_mdot_float(reset != 0);
+    case 1: return lmg::bounds_status_mdot_double(reset != 0);
+    case 2: return lmg::bounds_status_sym(reset != 0);
+    default: return lmg::bounds_status_here(reset != 0);
+  }
+}
+
+// Runs a check that fails on purpose without any access (which = 3 then
+// reads it back); returns the CUDA status.
+int lmg_internal_bounds_probe(void) {
+  bounds_probe_kernel<<<1, 32>>>(1000);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return (int)e;
 }
 
 // Timeline of the next symmetric-kernel launches (measurement hook, off when
