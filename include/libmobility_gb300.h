@@ -139,6 +139,17 @@ lmg_status lmg_get_include_angular(const lmg_solver *h, int *out);
 lmg_status lmg_mdot(lmg_solver *h, const void *F, size_t nF, const void *T,
                     size_t nT, void *U, size_t nU, void *W, size_t nW);
 
+/* Rows [row_begin, row_end) of NBody::Mdot (mobility.h:166-182): F and T hold
+ * all N particles (3N values each, either may be NULL), U and W receive the
+ * rows only (3 * (row_end - row_begin) values each, OVERWRITTEN).  Row i of
+ * the result sums every particle of i's batch, exactly like lmg_mdot; it is
+ * the matrix-vector product of one rank of a row-partitioned Lanczos solve
+ * (the reference's Lanczos is single-device: include/lanczos/
+ * LanczosAlgorithm.cu:173-232 calls the whole Mdot).  NBody solvers only. */
+lmg_status lmg_mdot_rows(lmg_solver *h, int64_t row_begin, int64_t row_end,
+                         const void *F, size_t nF, const void *T, size_t nT,
+                         void *U, size_t nU, void *W, size_t nW);
+
 /* Mobility::sqrtMdotW -- MobilityInterface.h:132-188 with the Lanczos solver
  * of include/lanczos/LanczosAlgorithm.cu:173-232.  ADDS prefactor*sqrt(M) dW
  * into U (and W), dW drawn from the handle's seeded generator. */

@@ -42,6 +42,8 @@ SIGNATURES = {
     "lmg_get_number_particles": (_I, [_VP, ctypes.POINTER(ctypes.c_int64)]),
     "lmg_get_include_angular": (_I, [_VP, ctypes.POINTER(_I)]),
     "lmg_mdot": (_I, [_VP, _VP, _SZ, _VP, _SZ, _VP, _SZ, _VP, _SZ]),
+    "lmg_mdot_rows": (_I, [_VP, ctypes.c_int64, ctypes.c_int64, _VP, _SZ, _VP, _SZ, _VP, _SZ,
+                           _VP, _SZ]),
     "lmg_sqrt_mdot_w": (_I, [_VP, _VP, _SZ, _VP, _SZ, _D]),
     "lmg_sqrt_mdot_w_noise": (_I, [_VP, _VP, _SZ, _VP, _SZ, _VP, _SZ, _D,
                                    ctypes.POINTER(_I), ctypes.POINTER(_D)]),

@@ -157,6 +157,14 @@ lmg_status lmg_mdot(lmg_solver *h, const void *F, size_t nF, const void *T, size
   return guarded(h, [&](lmg::SolverBase &m) { m.mdot(F, nF, T, nT, U, nU, W, nW); });
 }
 
+lmg_status lmg_mdot_rows(lmg_solver *h, int64_t row_begin, int64_t row_end, const void *F,
+                         size_t nF, const void *T, size_t nT, void *U, size_t nU, void *W,
+                         size_t nW) {
+  return guarded(h, [&](lmg::SolverBase &m) {
+    m.mdot_rows(row_begin, row_end, F, nF, T, nT, U, nU, W, nW);
+  });
+}
+
 lmg_status lmg_sqrt_mdot_w(lmg_solver *h, void *U, size_t nU, void *W, size_t nW,
                            double prefactor) {
   return guarded(h, [&](lmg::SolverBase &m) {

@@ -45,6 +45,9 @@ template <class R> struct MdotArgs {
   const int *sys_begin;  // optional table of batch starts (nsys+1 entries)
   int nsys;              // number of entries-1 in sys_begin, or 0
   int N;                 // particles
+  // targets [tgt_begin, tgt_end) (tgt_end = 0: all N), results written at
+  // row i - tgt_begin of U and W (every source of a target's batch counts)
+  int tgt_begin, tgt_end;
   int nper;              // equal batch size when sys_begin == nullptr
   int chunk;             // sources per split (multiple of THREADS)
   R inv_a;               // 1/a
@@ -217,10 +220,11 @@ mdot_kernel(const MdotArgs<R> a) {
   __shared__ int s_last;
 
   const int N = a.N;
+  const int t_lo = a.tgt_begin, t_hi = a.tgt_end > 0 ? a.tgt_end : N;
   const int tile = blockIdx.x;
   const int split = blockIdx.y;
   const int nsplit = gridDim.y;
-  const int tgt0 = tile * BT;
+  const int tgt0 = t_lo + tile * BT;
   const R ia = a.inv_a;
 
   // ---- targets ----
@@ -229,7 +233,7 @@ mdot_kernel(const MdotArgs<R> a) {
 #pragma unroll
   for (int t = 0; t < TPT; t++) {
     int i = tgt0 + threadIdx.x + t * THREADS;
-    int ic = i < N ? i : N - 1;
+    int ic = i < t_hi ? i : t_hi - 1;
     R x = a.pos[3 * ic], y = a.pos[3 * ic + 1], z = a.pos[3 * ic + 2];
     xi[t] = mul_rn(x, ia);
     yi[t] = mul_rn(y, ia);
@@ -246,7 +250,7 @@ mdot_kernel(const MdotArgs<R> a) {
     hi[t] = system_end(a, s);
   }
   // batch range of the whole CTA
-  const int last = (tgt0 + BT < N ? tgt0 + BT : N) - 1;
+  const int last = (tgt0 + BT < t_hi ? tgt0 + BT : t_hi) - 1;
   const int s_first = system_of(a, tgt0);
   const int s_lastb = system_of(a, last);
   const int src_lo = system_start(a, s_first);
@@ -511,16 +515,17 @@ mdot_kernel(const MdotArgs<R> a) {
 #pragma unroll
     for (int t = 0; t < TPT; t++) {
       const int i = tgt0 + threadIdx.x + t * THREADS;
-      if (i >= N) continue;
+      if (i >= t_hi) continue;
+      const int o = i - t_lo;  // output row
       if (a.U && LMG_IN_BOUNDS(i < N, 5, i)) {
-        a.U[3 * i] = bi[t] * (S[t][0] + C[t][0]);
-        a.U[3 * i + 1] = bi[t] * (S[t][1] + C[t][1]);
-        a.U[3 * i + 2] = bi[t] * (S[t][2] + C[t][2]);
+        a.U[3 * o] = bi[t] * (S[t][0] + C[t][0]);
+        a.U[3 * o + 1] = bi[t] * (S[t][1] + C[t][1]);
+        a.U[3 * o + 2] = bi[t] * (S[t][2] + C[t][2]);
       }
-      if (ANG && a.W) {
-        a.W[3 * i] = bi[t] * (S[t][NC - 3] + C[t][NC - 3]);
-        a.W[3 * i + 1] = bi[t] * (S[t][NC - 2] + C[t][NC - 2]);
-        a.W[3 * i + 2] = bi[t] * (S[t][NC - 1] + C[t][NC - 1]);
+      if (ANG && a.W && LMG_IN_BOUNDS(i < N, 5, i)) {
+        a.W[3 * o] = bi[t] * (S[t][NC - 3] + C[t][NC - 3]);
+        a.W[3 * o + 1] = bi[t] * (S[t][NC - 2] + C[t][NC - 2]);
+        a.W[3 * o + 2] = bi[t] * (S[t][NC - 1] + C[t][NC - 1]);
       }
     }
     return;
@@ -588,16 +593,17 @@ mdot_kernel(const MdotArgs<R> a) {
         }
       }
     }
-    if (i < N) {
+    if (i < t_hi) {
+      const int o = i - t_lo;  // output row
       if (a.U && LMG_IN_BOUNDS(i < N, 5, i)) {
-        a.U[3 * i] = bi[t] * (Ss[0] + Cs[0]);
-        a.U[3 * i + 1] = bi[t] * (Ss[1] + Cs[1]);
-        a.U[3 * i + 2] = bi[t] * (Ss[2] + Cs[2]);
+        a.U[3 * o] = bi[t] * (Ss[0] + Cs[0]);
+        a.U[3 * o + 1] = bi[t] * (Ss[1] + Cs[1]);
+        a.U[3 * o + 2] = bi[t] * (Ss[2] + Cs[2]);
       }
-      if (ANG && a.W) {
-        a.W[3 * i] = bi[t] * (Ss[NC - 3] + Cs[NC - 3]);
-        a.W[3 * i + 1] = bi[t] * (Ss[NC - 2] + Cs[NC - 2]);
-        a.W[3 * i + 2] = bi[t] * (Ss[NC - 1] + Cs[NC - 1]);
+      if (ANG && a.W && LMG_IN_BOUNDS(i < N, 5, i)) {
+        a.W[3 * o] = bi[t] * (Ss[NC - 3] + Cs[NC - 3]);
+        a.W[3 * o + 1] = bi[t] * (Ss[NC - 2] + Cs[NC - 2]);
+        a.W[3 * o + 2] = bi[t] * (Ss[NC - 1] + Cs[NC - 1]);
       }
     }
   }

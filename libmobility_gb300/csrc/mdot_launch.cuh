@@ -27,8 +27,11 @@ cudaError_t mdot_launch(const MdotShape &s, const MdotArgs<R> &args, const MdotP
                         cudaStream_t stream);
 
 // Longest source range needed by a tile of `bt` consecutive targets (batches
-// of nper, or the explicit batch table `sys_begin` of nsys batches).
-inline int mdot_max_span(int N, int nper, const int *sys_begin_host, int nsys, int bt) {
+// of nper, or the explicit batch table `sys_begin` of nsys batches), tiles
+// starting at target t_lo and ending before t_hi (0: N).
+inline int mdot_max_span(int N, int nper, const int *sys_begin_host, int nsys, int bt,
+                         int t_lo = 0, int t_hi = 0) {
+  if (t_hi <= 0) t_hi = N;
   auto sys_of = [&](int i) {
     if (!sys_begin_host) return i / nper;
     int lo = 0, hi = nsys;
@@ -45,8 +48,8 @@ inline int mdot_max_span(int N, int nper, const int *sys_begin_host, int nsys, i
   };
   if (!sys_begin_host && nper >= N) return N;
   int span = 0;
-  for (int t0 = 0; t0 < N; t0 += bt) {
-    int last = std::min(N, t0 + bt) - 1;
+  for (int t0 = t_lo; t0 < t_hi; t0 += bt) {
+    int last = std::min(t_hi, t0 + bt) - 1;
     span = std::max(span, end(sys_of(last)) - start(sys_of(t0)));
   }
   return span;

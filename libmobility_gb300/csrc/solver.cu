@@ -105,6 +105,8 @@ template <class R> class Solver final : public SolverBase {
   void set_positions(const void *pos, size_t n) override;
   void mdot(const void *F, size_t nF, const void *T, size_t nT, void *U, size_t nU, void *W,
             size_t nW) override;
+  void mdot_rows(int64_t row_begin, int64_t row_end, const void *F, size_t nF, const void *T,
+                 size_t nT, void *U, size_t nU, void *W, size_t nW) override;
   void sqrt_mdot_w(void *U, size_t nU, void *W, size_t nW, double prefactor, const void *dW,
                    size_t ndW, int *iterations, double *residual) override;
   void div_m(void *U, size_t nU, void *W, size_t nW, double prefactor) override;
@@ -190,8 +192,13 @@ template <class R> class Solver final : public SolverBase {
   size_t red_half() const { return red_part_.count / 2; }
   void ensure_side();
   const R *device_input(const void *p, size_t n, R *stage);
-  // M . [F;T] on device buffers: the Lanczos matvec and the RFD probes
-  void mdot_device(const R *pos, const R *F, const R *T, R *U, R *W);
+  // M . [F;T] on device buffers: the Lanczos matvec and the RFD probes; with
+  // row_end > 0 only targets [row_begin, row_end), written from row 0 of U, W
+  void mdot_device(const R *pos, const R *F, const R *T, R *U, R *W, int row_begin = 0,
+                   int row_end = 0);
+  void mdot_rows_device(const R *pos, const R *F, const R *T, R *U, R *W, int row_begin,
+                        int row_end);
+  std::map<std::tuple<int, int, int, int, int>, MdotPlan> row_plans_;
   int lanczos(const R *z, R *y, size_t n, double tol, double *residual);
   bool prec_active() const;
   void prec_build();
@@ -215,6 +222,7 @@ template <class R> void Solver<R>::release_all() {
   cvec_.release(); mirror_.release(); hc_.release(); quad_g_.release(); ql_work_ = {}; rot_cs_ = {}; rot_idx_ = {};
   h_dbl_.release(); rfd_noise_.release(); rfd_pos_.release(); rfd_mp_.release(); rfd_mm_.release();
   plans_.clear();
+  row_plans_.clear();
   sym_plans_.clear();
   sym_err_.release();
   tickets_zeroed_ = false;
@@ -307,7 +315,13 @@ template <class R> const R *Solver<R>::device_input(const void *p, size_t n, R *
 }
 
 template <class R>
-void Solver<R>::mdot_device(const R *pos, const R *F, const R *T, R *U, R *W) {
+void Solver<R>::mdot_device(const R *pos, const R *F, const R *T, R *U, R *W, int row_begin,
+                            int row_end) {
+  const bool rows = row_end > 0 && !(row_begin == 0 && row_end == (int)N_);
+  if (rows) {
+    mdot_rows_device(pos, F, T, U, W, row_begin, row_end);
+    return;
+  }
   MdotShape s;
   s.geom = wall_ ? kWall : kOpen;
   s.ang = ang_;
@@ -358,6 +372,100 @@ void Solver<R>::mdot_device(const R *pos, const R *F, const R *T, R *U, R *W) {
   a.part = part_.ptr;
   a.ticket = tickets_.ptr;
   LMG_CUDA(mdot_launch<R>(s, a, plan, stream()));
+}
+
+// Targets [row_begin, row_end) only, with the tiled kernel: every source of
+// a target's batch counts, results from row 0 of U and W.
+template <class R>
+void Solver<R>::mdot_rows_device(const R *pos, const R *F, const R *T, R *U, R *W,
+                                 int row_begin, int row_end) {
+  MdotShape s;
+  s.geom = wall_ ? kWall : kOpen;
+  s.ang = ang_;
+  s.has_f = F != nullptr;
+  s.has_t = T != nullptr && ang_;
+  const int N = (int)N_, rows = row_end - row_begin;
+  if (!s.has_f && !s.has_t) {
+    if (U) LMG_CUDA(cudaMemsetAsync(U, 0, 3 * (size_t)rows * sizeof(R), stream()));
+    if (W) LMG_CUDA(cudaMemsetAsync(W, 0, 3 * (size_t)rows * sizeof(R), stream()));
+    return;
+  }
+  const int shape = (s.geom << 3) | (s.has_f << 2) | (s.has_t << 1) | (int)s.ang;
+  const auto key = std::make_tuple(N, row_begin, row_end, batch_size(), shape);
+  auto it = row_plans_.find(key);
+  if (it == row_plans_.end()) {
+    MdotPlan plan;
+    LMG_CUDA(mdot_plan<R>(s, rows, N, sms(), 0, 0, plan));
+    const int span = mdot_max_span(N, batch_size(), nullptr, 0, plan.threads * plan.tpt,
+                                   row_begin, row_end);
+    LMG_CUDA(mdot_plan<R>(s, rows, span, sms(), plan.tpt, 0, plan));
+    it = row_plans_.insert_or_assign(key, plan).first;
+  }
+  const MdotPlan &plan = it->second;
+  if (plan.nsplit > 1) {
+    part_.ensure(plan.part_elems);
+    if (tickets_.count < plan.tickets || !tickets_zeroed_) {
+      tickets_.ensure(std::max(plan.tickets, tickets_.count));
+      LMG_CUDA(cudaMemsetAsync(tickets_.ptr, 0, tickets_.count * sizeof(unsigned), stream()));
+      tickets_zeroed_ = true;
+    }
+  }
+  MdotArgs<R> a{};
+  a.pos = pos;
+  a.F = F;
+  a.T = s.has_t ? T : nullptr;
+  a.U = U;
+  a.W = ang_ ? W : nullptr;
+  a.N = N;
+  a.nper = batch_size();
+  a.tgt_begin = row_begin;
+  a.tgt_end = row_end;
+  a.inv_a = (R)(1.0 / a_);
+  a.k = make_pair_const<R>(t0_, r0_, rt0_);
+  a.kw = make_wall_const(t0_, r0_, rt0_);
+  a.part = part_.ptr;
+  a.ticket = tickets_.ptr;
+  LMG_CUDA(mdot_launch<R>(s, a, plan, stream()));
+}
+
+template <class R>
+void Solver<R>::mdot_rows(int64_t row_begin, int64_t row_end, const void *F, size_t nF,
+                          const void *T, size_t nT, void *U, size_t nU, void *W, size_t nW) {
+  NvtxRange nvtx_range_("lmg Mdot rows");
+  if (!F) nF = 0;
+  if (!T) nT = 0;
+  if (!U) nU = 0;
+  if (!W) nW = 0;
+  check_positions_set("Mdot");
+  if (row_begin < 0 || row_end <= row_begin || row_end > N_)
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] rows must satisfy 0 <= row_begin < row_end <= N");
+  check_mdot_args(nF, nT, 0, 0);
+  const size_t n3 = 3 * (size_t)N_, r3 = 3 * (size_t)(row_end - row_begin);
+  if ((nU && nU != r3) || (nW && nW != r3))
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] row outputs must have 3 * (row_end - row_begin) values");
+  R *stage = in_stage_.ensure(2 * n3);
+  out_stage_.ensure(2 * n3);
+  pin_.ensure(2 * n3);
+  const R *Fd = device_input(F, nF, stage);
+  const R *Td = device_input(T, nT, stage + n3);
+  const bool u_dev = nU && is_device_ptr(U);
+  const bool w_dev = nW && is_device_ptr(W);
+  R *Ud = nU ? (u_dev ? static_cast<R *>(U) : out_stage_.ensure(2 * n3)) : nullptr;
+  R *Wd = nW ? (w_dev ? static_cast<R *>(W) : out_stage_.ensure(2 * n3) + n3) : nullptr;
+  mdot_rows_device(pos_.ptr, Fd, Td, Ud, Wd, (int)row_begin, (int)row_end);
+  LMG_CUDA(cudaGetLastError());
+  if ((nU && !u_dev) || (nW && !w_dev)) {
+    R *h = pin_.ensure(2 * n3);
+    if (nU && !u_dev)
+      LMG_CUDA(cudaMemcpyAsync(h, Ud, r3 * sizeof(R), cudaMemcpyDeviceToHost, stream()));
+    if (nW && !w_dev)
+      LMG_CUDA(cudaMemcpyAsync(h + n3, Wd, r3 * sizeof(R), cudaMemcpyDeviceToHost, stream()));
+    LMG_CUDA(cudaStreamSynchronize(stream()));
+    if (nU && !u_dev) std::memcpy(U, h, r3 * sizeof(R));
+    if (nW && !w_dev) std::memcpy(W, h + n3, r3 * sizeof(R));
+  }
 }
 
 // U = M F with the symmetric open-space kernel (FP32, forces only, no

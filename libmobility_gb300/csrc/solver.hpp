@@ -43,6 +43,15 @@ class SolverBase {
   virtual void set_positions(const void *pos, size_t n) = 0;
   virtual void mdot(const void *F, size_t nF, const void *T, size_t nT, void *U, size_t nU,
                     void *W, size_t nW) = 0;
+  // Rows [row_begin, row_end) of M.[F;T] (F, T of all N particles; U, W of
+  // the rows only): the product of one rank of a row-partitioned solve.
+  virtual void mdot_rows(int64_t row_begin, int64_t row_end, const void *F, size_t nF,
+                         const void *T, size_t nT, void *U, size_t nU, void *W, size_t nW) {
+    (void)row_begin; (void)row_end; (void)F; (void)nF; (void)T; (void)nT;
+    (void)U; (void)nU; (void)W; (void)nW;
+    throw Error(LMG_ERR_INVALID_ARGUMENT,
+                "[libmobility_gb300] row products are available for NBody solvers only");
+  }
   virtual void sqrt_mdot_w(void *U, size_t nU, void *W, size_t nW, double prefactor,
                            const void *dW, size_t ndW, int *iterations, double *residual) = 0;
   virtual void div_m(void *U, size_t nU, void *W, size_t nW, double prefactor) = 0;

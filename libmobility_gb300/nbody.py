@@ -299,6 +299,38 @@ class NBody:
             ctypes.c_void_p(t.ptr) if t else None, t.size if t else 0, up, un, wp, wn))
         return mf, mt
 
+    def Mdot_rows(self, row_begin, row_end, forces=None, torques=None):
+        """Rows [row_begin, row_end) of M.[F;T] for forces/torques of all N
+        particles -> (linear, angular), each of shape (row_end - row_begin, 3);
+        the product of one rank of a row-partitioned solve (no counterpart in
+        the reference, whose Mdot is solvers/NBody/mobility.h:166-182)."""
+        f = self._arr(forces)
+        t = self._arr(torques)
+        N = self.getNumberParticles()
+        if f is not None and f.size != 3 * N:
+            raise RuntimeError("The forces array must have size 3*N.")
+        if t is not None and t.size != 3 * N:
+            raise RuntimeError("The torques array must have size 3*N.")
+        if t is not None and not self._include_angular:
+            raise RuntimeError(
+                "The solver was configured without including angular velocities. Set "
+                "includeAngular to true when initializing if you want to use torques")
+        src = f if f is not None else t
+        if src is None:
+            raise RuntimeError("[libMobility] Mdot needs forces and/or torques")
+        rows = int(row_end) - int(row_begin)
+        shape = (max(rows, 0), 3)
+        mf = self._zeros(shape, src.framework, src.device)
+        mt = self._zeros(shape, src.framework, src.device) if self._include_angular else None
+        self._bind_stream(f, t)
+        up, un = self._ptr(mf)
+        wp, wn = self._ptr(mt)
+        self._check(self._lib.lmg_mdot_rows(
+            self._h, int(row_begin), int(row_end),
+            ctypes.c_void_p(f.ptr) if f else None, f.size if f else 0,
+            ctypes.c_void_p(t.ptr) if t else None, t.size if t else 0, up, un, wp, wn))
+        return mf, mt
+
     def _fresh_outputs(self):
         mf = self._zeros(self._last_shape, self._last_framework, self._last_device)
         mt = (self._zeros(self._last_shape, self._last_framework, self._last_device)
