@@ -126,6 +126,8 @@ def load():
         "lmg_internal_barrier_timeout_probe": [_VP],
         "lmg_internal_sym_override": [_I, _I],
         "lmg_internal_sym_trace": [_VP],
+        "lmg_internal_lanczos_step_mode": [_I],
+        "lmg_internal_lanczos_step_shape": [_I, _I],
         "lmg_internal_classify_pointer": [_I, _I, _I],
         "lmg_internal_lanczos_device_sqrt": [_I],
         "lmg_internal_lanczos_lookahead": [_I],

@@ -257,6 +257,260 @@ krylov_step_kernel(R *w, const R *vi, const R *vprev, R *vnext, size_t n, int i,
 }
 
 // ---------------------------------------------------------------------------
+// Thread-block cluster helpers: the CTA's rank in its cluster and the
+// cluster's CTA count, the split cluster barrier (arrive with release
+// semantics, wait with acquire semantics; every thread of every CTA takes
+// part, and the hardware guarantees that the CTAs of a cluster run at the
+// same time) and FP64 loads from another CTA's shared memory.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned cluster_ctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_nctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_arrive() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// *local as it is in the shared memory of the cluster's CTA `rank`
+__device__ __forceinline__ double ld_dsmem(const double *local, unsigned rank) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+  unsigned ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(ra) : "memory");
+  return v;
+}
+
+constexpr int kClusterThreads = 1024;
+
+__device__ __forceinline__ float2 ld_dsmem(const float2 *local, unsigned rank) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+  unsigned ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(ra)
+               : "memory");
+  return v;
+}
+
+// Per-thread sums of products for the cluster reductions.  FP64 vectors sum
+// in FP64.  FP32 vectors sum as an unevaluated pair of floats s + c
+// ("double-float": each product's rounding error from an fma, each
+// addition's from Knuth's two-sum; Ogita, Rump and Oishi, SIAM J. Sci.
+// Comput. 26, 2005), good to about 2^-48 relative: GB300 runs FP64 at a small
+// fraction of its FP32 rate, and FP64 accumulation on the few SMs of one
+// cluster would bound these kernels.
+template <class R> struct DotAcc {
+  double v = 0.0;
+  __device__ __forceinline__ void add_prod(R x, R y) { v += (double)x * (double)y; }
+  __device__ __forceinline__ void warp_merge() { v = warp_sum(v); }
+  __device__ __forceinline__ double value() const { return v; }
+};
+template <> struct DotAcc<float> {
+  float s = 0.f, c = 0.f;
+  // s + c += p + pe, where p + pe is exact and |pe| is below an ulp of p
+  __device__ __forceinline__ void add(float p, float pe) {
+    const float t = __fadd_rn(s, p);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, pe));
+  }
+  __device__ __forceinline__ void add_prod(float x, float y) {
+    const float p = __fmul_rn(x, y);
+    add(p, __fmaf_rn(x, y, -p));
+  }
+  // (s, c) += (s2, c2); the same result for either order of the operands
+  __device__ __forceinline__ void merge(float s2, float c2) {
+    const float t = __fadd_rn(s, s2);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(s2, bp));
+    s = t;
+    c = __fadd_rn(__fadd_rn(c, c2), err);
+  }
+  __device__ __forceinline__ void warp_merge() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      merge(__shfl_xor_sync(0xffffffffu, s, o), __shfl_xor_sync(0xffffffffu, c, o));
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// Shared memory of the cluster reductions: per-warp sums, this CTA's sums
+// (one slot per reduction of a launch, read by the other CTAs) and totals.
+template <class R> struct ClusterRed {
+  double warp[32];
+  double part[2];
+  double tot[2];
+  __device__ __forceinline__ void put_warp(int w, const DotAcc<R> &a) { warp[w] = a.v; }
+  __device__ __forceinline__ DotAcc<R> get_warp(int w) const { DotAcc<R> a; a.v = warp[w]; return a; }
+  __device__ __forceinline__ void put_part(int q, const DotAcc<R> &a) { part[q] = a.v; }
+  __device__ __forceinline__ DotAcc<R> get_part(int q, unsigned rank) const {
+    DotAcc<R> a;
+    a.v = ld_dsmem(&part[q], rank);
+    return a;
+  }
+};
+template <> struct ClusterRed<float> {
+  float2 warp[32];
+  float2 part[2];
+  double tot[2];
+  __device__ __forceinline__ void put_warp(int w, const DotAcc<float> &a) {
+    warp[w] = make_float2(a.s, a.c);
+  }
+  __device__ __forceinline__ DotAcc<float> get_warp(int w) const {
+    DotAcc<float> a;
+    a.s = warp[w].x;
+    a.c = warp[w].y;
+    return a;
+  }
+  __device__ __forceinline__ void put_part(int q, const DotAcc<float> &a) {
+    part[q] = make_float2(a.s, a.c);
+  }
+  __device__ __forceinline__ DotAcc<float> get_part(int q, unsigned rank) const {
+    const float2 v = ld_dsmem(&part[q], rank);
+    DotAcc<float> a;
+    a.s = v.x;
+    a.c = v.y;
+    return a;
+  }
+};
+
+// The sum over the cluster of every thread's accumulator, the same value in
+// every thread of every CTA: xor trees within the warps, over the block's
+// warps (warp 0) and over the cluster's CTAs (warp 0, reading the other CTAs'
+// partials in distributed shared memory after a cluster barrier), then
+// broadcast through shared memory.  Each reduction of a launch uses its own
+// partial slot `q`, so no CTA overwrites a partial that another may still
+// be reading.
+template <class R>
+__device__ __forceinline__ double cluster_reduce(DotAcc<R> a, ClusterRed<R> &sh, int q,
+                                                 unsigned nct) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  a.warp_merge();
+  if (lane == 0) sh.put_warp(wid, a);
+  __syncthreads();
+  if (wid == 0) {
+    DotAcc<R> b;
+    if (lane < (int)(blockDim.x >> 5)) b = sh.get_warp(lane);
+    b.warp_merge();
+    if (lane == 0) sh.put_part(q, b);
+  }
+  cluster_arrive();
+  cluster_wait();
+  if (wid == 0) {
+    DotAcc<R> b;
+    if (lane < (int)nct) b = sh.get_part(q, lane);
+    b.warp_merge();
+    if (lane == 0) sh.tot[q] = b.value();
+  }
+  __syncthreads();
+  return sh.tot[q];
+}
+
+// ---------------------------------------------------------------------------
+// The vector work of one Lanczos iteration after the matvec (the same three
+// phases and per-element arithmetic as krylov_step_kernel; FP32 vectors
+// accumulate their inner products in double-float, see DotAcc) in ONE
+// thread-block cluster: the two reductions go through distributed shared memory and the
+// hardware cluster barrier instead of global partials, tickets and software
+// grid barriers, so the launch has no spin-wait and leaves the rest of the
+// GPU free (the convergence check on the side stream runs beside it).  With
+// EPT > 0 each thread keeps its EPT elements of w and v_i in registers
+// across the phases (n <= EPT x the cluster's threads); EPT = 0 streams them
+// through memory (any n).  Launched as one cluster of up to 16 CTAs of up
+// to kClusterThreads threads (a multiple of 32).
+// ---------------------------------------------------------------------------
+template <class R, int EPT>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+krylov_step_cluster_kernel(R *w, const R *vi, const R *vprev, R *vnext, size_t n, int i,
+                           KrylovScalars *sc, double *host_ab) {
+  __shared__ ClusterRed<R> red;
+  constexpr int E = EPT > 0 ? EPT : 1;
+  const unsigned nct = cluster_nctarank(), rank = cluster_ctarank();
+  const size_t stride = (size_t)nct * blockDim.x;
+  const size_t e0 = (size_t)rank * blockDim.x + threadIdx.x;
+  R wr[E], vr[E];
+  // w -= beta_{i-1} v_{i-1};  alpha_i = w . v_i
+  const R bprev = i > 0 ? (R)sc->beta[i - 1] : R(0);
+  DotAcc<R> acc;
+  if (EPT > 0) {
+#pragma unroll
+    for (int k = 0; k < E; k++) {
+      const size_t e = e0 + (size_t)k * stride;
+      wr[k] = vr[k] = R(0);
+      if (e < n) {
+        R x = w[e];
+        if (i > 0) x -= bprev * vprev[e];
+        wr[k] = x;
+        vr[k] = vi[e];
+        acc.add_prod(x, vr[k]);
+      }
+    }
+  } else {
+    for (size_t e = e0; e < n; e += stride) {
+      R x = w[e];
+      if (i > 0) x -= bprev * vprev[e];
+      w[e] = x;
+      acc.add_prod(x, vi[e]);
+    }
+  }
+  const double alpha = cluster_reduce<R>(acc, red, 0, nct);
+  // w -= alpha_i v_i;  beta_i = |w| with the breakdown rule
+  const R al = (R)alpha;
+  DotAcc<R> acc2;
+  if (EPT > 0) {
+#pragma unroll
+    for (int k = 0; k < E; k++) {
+      if (e0 + (size_t)k * stride < n) {
+        const R x = wr[k] - al * vr[k];
+        wr[k] = x;
+        acc2.add_prod(x, x);
+      }
+    }
+  } else {
+    for (size_t e = e0; e < n; e += stride) {
+      const R x = w[e] - al * vi[e];
+      w[e] = x;
+      acc2.add_prod(x, x);
+    }
+  }
+  double b = sqrt(cluster_reduce<R>(acc2, red, 1, nct));
+  // no CTA reads another's partials after this point; the matching wait
+  // before the exit keeps every CTA's shared memory alive until then
+  cluster_arrive();
+  const double tol = 1e-3 * alpha / sc->normz;  // LanczosAlgorithm.cu:141-143
+  if (b < tol) b = 0.0;
+  if (rank == 0 && threadIdx.x == 0) {
+    sc->alpha[i] = alpha;
+    sc->beta[i] = b;
+    host_ab[2 * i] = alpha;
+    host_ab[2 * i + 1] = b;
+  }
+  // v_{i+1} = w / beta_i, or e1 after a breakdown
+  const R inv = b > 0.0 ? (R)(1.0 / b) : R(0);
+  if (EPT > 0) {
+#pragma unroll
+    for (int k = 0; k < E; k++) {
+      const size_t e = e0 + (size_t)k * stride;
+      if (e < n) vnext[e] = b > 0.0 ? wr[k] * inv : (e == 0 ? R(1) : R(0));
+    }
+  } else {
+    for (size_t e = e0; e < n; e += stride)
+      vnext[e] = b > 0.0 ? w[e] * inv : (e == 0 ? R(1) : R(0));
+  }
+  cluster_wait();
+}
+
+// ---------------------------------------------------------------------------
 // T_m^{1/2} e1 in FP64: implicit QL with Wilkinson shifts on the symmetric
 // tridiagonal T_m (the tql1/tql2 family of Bowdler, Martin, Reinsch and
 // Wilkinson, Numer. Math. 11, 1968).  Only the first row of the eigenvector
@@ -475,7 +729,6 @@ inline int tridiag_sqrt_e1_quad(const double *alpha, const double *beta, int m, 
   return 0;
 }
 
-// y = |z| V_m c   (V row-major: row k is v_k, n elements)
 // ---------------------------------------------------------------------------
 // T^{1/2} e1 on the device, by the quadrature of tridiag_sqrt_e1_quad (same
 // spectrum bounds, node rule, weights and node order), so that a convergence
@@ -626,32 +879,32 @@ tridiag_sqrt_quad_kernel(const KrylovScalars *sc, int m, double *out, double *G,
   if (t == 0) *flag = 0.0;
 }
 
+// y = |z| V c over m basis vectors and, when yprev is given, err = |y -
+// yprev| / |yprev| (FP64) -> sc->err and the mapped host copy: the estimate
+// and the error of one convergence check in one launch (each thread's
+// elements of y feed its share of the error sums directly).  V is row-major
+// (row k is v_k, ldv elements apart); c may live in mapped host memory.
 template <class R>
-__global__ void krylov_estimate_kernel(const R *V, size_t ldv, int m, const double *c,
-                                       const KrylovScalars *sc, R *y, size_t n) {
+__global__ void krylov_check_kernel(const R *V, size_t ldv, int m, const double *c,
+                                    KrylovScalars *sc, R *y, const R *yprev, size_t n,
+                                    double *partials, unsigned *ticket, double *host_err) {
   __shared__ R cs[256];
   const double nz = sc->normz;
   for (int k = threadIdx.x; k < m; k += blockDim.x) cs[k] = (R)(nz * c[k]);
   __syncthreads();
+  double v[2] = {0.0, 0.0};
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
        e += (size_t)gridDim.x * blockDim.x) {
     R acc = 0;
     for (int k = 0; k < m; k++) acc += cs[k] * V[(size_t)k * ldv + e];
     y[e] = acc;
+    if (yprev) {
+      const double a = (double)yprev[e], dlt = (double)acc - a;
+      v[0] += a * a;
+      v[1] += dlt * dlt;
+    }
   }
-}
-
-// err = |y - yprev| / |yprev| (FP64) -> sc->err and the mapped host copy
-template <class R>
-__global__ void krylov_error_kernel(const R *y, const R *yprev, size_t n, double *partials,
-                                    unsigned *ticket, KrylovScalars *sc, double *host_err) {
-  double v[2] = {0.0, 0.0};
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const double a = (double)yprev[e], dlt = (double)y[e] - a;
-    v[0] += a * a;
-    v[1] += dlt * dlt;
-  }
+  if (!yprev) return;
   double tot[2];
   if (grid_sum<2>(v, partials, ticket, tot)) {
     const double err = fabs(sqrt(tot[1]) / sqrt(tot[0]));

@@ -13,11 +13,18 @@ extern std::atomic<int> g_force_tpt, g_force_split;
 // g_sym_warps > 0 caps the warps its steps are spread over; g_sym_variant is
 // its register budget, 2, 3 or 4 resident blocks per SM (0 = default, 2)
 extern std::atomic<int> g_sym_mode, g_sym_warps, g_sym_variant;
-// T^{1/2} e1 of the single-system Lanczos checks: 0 (default) the exact host
-// QL; 1 on the device by quadrature, the host QL where that falls back
+// T^{1/2} e1 of the single-system Lanczos checks: 0 the exact host QL; 1 on
+// the device by quadrature; 2 (default) on the host by quadrature; the host
+// QL wherever a quadrature falls back
 extern std::atomic<int> g_lanczos_device_sqrt;
 // iterations issued ahead of a check (0 = by batch size: 3 up to 8192 particles, else 1)
 extern std::atomic<int> g_lanczos_lookahead;
+// the single-system Lanczos vector step: 0 (default) one thread-block
+// cluster, 1 the cooperative grid-wide launch
+extern std::atomic<int> g_lanczos_step_mode;
+// its cluster shape, (CTAs << 16) | threads per CTA (0 = the largest cluster
+// of kClusterThreads-thread CTAs that fits)
+extern std::atomic<int> g_lanczos_step_shape;
 // device buffer for the symmetric kernel's timeline (null = off)
 extern std::atomic<unsigned long long *> g_sym_trace;
 }  // namespace lmg

@@ -23,8 +23,10 @@ std::atomic<unsigned long long> g_launches{0};
 std::atomic<int> g_force_tpt{0}, g_force_split{0};
 std::atomic<int> g_sym_mode{0}, g_sym_warps{0}, g_sym_variant{0};
 std::atomic<unsigned long long *> g_sym_trace{nullptr};
-std::atomic<int> g_lanczos_device_sqrt{0};
+std::atomic<int> g_lanczos_device_sqrt{2};
 std::atomic<int> g_lanczos_lookahead{0};
+std::atomic<int> g_lanczos_step_mode{0};
+std::atomic<int> g_lanczos_step_shape{0};
 }
 
 namespace {
@@ -163,15 +165,16 @@ int lmg_internal_sym_plan(int N, int nper, long long resident, int force_warps, 
   return 0;
 }
 
-// Where the single-system Lanczos takes T^{1/2} e1 at its checks: 0 (the
-// default) the exact QL on the host; 1 on the device by quadrature, with the
-// host QL where the quadrature does not apply.  Applies to the next solves
-// of every handle.  (Measured at N = 4096: 6.0 ms per solve on the host, 8.4
-// ms on the device: the quadrature is a chain of FP64 divisions, and its
-// kernels cannot overlap the cooperative matrix-vector and vector-step
-// launches, so every check's device time adds to the solve.)
+// Where the single-system Lanczos takes T^{1/2} e1 at its checks: 0 the
+// exact QL on the host; 1 on the device by quadrature; 2 (the default) on
+// the host by quadrature; the host QL wherever a quadrature does not apply.
+// Applies to the next solves of every handle.  (Measured at N = 4096, FP32,
+// tolerance 1e-6: 6.1 ms per solve with the host QL, 3.6 ms with the host
+// quadrature (18 against 296 us a check at m = 80 on a Grace core), 8.4 ms
+// on the device: there the quadrature is a chain of FP64 divisions on
+// GB300's narrow FP64 units.)
 int lmg_internal_lanczos_device_sqrt(int on) {
-  if (on != 0 && on != 1) return 1;
+  if (on < 0 || on > 2) return 1;
   lmg::g_lanczos_device_sqrt.store(on);
   return 0;
 }
@@ -218,6 +221,26 @@ int lmg_internal_bounds_probe(void) {
 // null): `buf` is device memory of 2 * (warps + blocks) 64-bit words, filled
 // with %globaltimer nanoseconds: per warp its start and the end of its
 // rotation steps, then per block the end of the grid barrier and of the fold.
+// Lanczos vector step of the single-system solver: 0 one cluster (default),
+// 1 the cooperative grid-wide launch.
+int lmg_internal_lanczos_step_mode(int mode) {
+  if (mode != 0 && mode != 1) return 1;
+  lmg::g_lanczos_step_mode.store(mode);
+  return 0;
+}
+
+// Cluster shape of that step: ctas in 1..16 and threads a multiple of 32 in
+// 32..1024, or 0, 0 for the default.
+int lmg_internal_lanczos_step_shape(int ctas, int threads) {
+  if (ctas == 0 && threads == 0) {
+    lmg::g_lanczos_step_shape.store(0);
+    return 0;
+  }
+  if (ctas < 1 || ctas > 16 || threads < 32 || threads > 1024 || threads % 32) return 1;
+  lmg::g_lanczos_step_shape.store((ctas << 16) | threads);
+  return 0;
+}
+
 int lmg_internal_sym_trace(void *buf) {
   lmg::g_sym_trace.store(static_cast<unsigned long long *>(buf));
   return 0;

@@ -128,7 +128,7 @@ template <class R> class Solver final : public SolverBase {
   DeviceBuffer<KrylovScalars> sc_;
   DeviceBuffer<double> cvec_;
   MappedBuffer<double> mirror_;       // (alpha_i, beta_i) pairs + err, device-written
-  PinnedBuffer<double> hc_;           // T^{1/2} e1 staged for the device (2 slots)
+  MappedBuffer<double> hc_;           // host T^{1/2} e1, read by the check kernel (2 slots)
   DeviceBuffer<double> quad_g_;       // node sums of the device square root
   std::vector<double> ql_work_;       // host QL work arrays
   std::vector<double2> rot_cs_;       // host QL rotation log
@@ -163,6 +163,7 @@ template <class R> class Solver final : public SolverBase {
   DeviceBuffer<float> ppad_;  // float4-padded work array of the P^T product
   int num_sms_ = 0;
   int step_per_sm_ = 0;  // resident krylov_step_kernel blocks per SM
+  int step_ctas_ = -1;   // CTAs of the cluster of krylov_step_cluster_kernel (0: none fits)
   bool tickets_zeroed_ = false;
   std::map<long, MdotPlan> plans_;
   // symmetric open-space product (FP32): plans with their device tables,
@@ -576,6 +577,78 @@ template <class R> void Solver<R>::ensure_side() {
   }
 }
 
+namespace {
+template <class R> const void *step_cluster_fn(int ept) {
+  switch (ept) {
+    case 1: return (const void *)krylov_step_cluster_kernel<R, 1>;
+    case 2: return (const void *)krylov_step_cluster_kernel<R, 2>;
+    case 4: return (const void *)krylov_step_cluster_kernel<R, 4>;
+    case 8: return (const void *)krylov_step_cluster_kernel<R, 8>;
+    default: return (const void *)krylov_step_cluster_kernel<R, 0>;
+  }
+}
+
+cudaLaunchConfig_t cluster_config(int ctas, int threads, cudaStream_t st,
+                                  cudaLaunchAttribute *at) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = ctas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+// The largest cluster (16, 8, 4, 2 CTAs of kClusterThreads) of the Krylov
+// step that fits on the current GPU; 0 if none does.
+template <class R> int step_cluster_ctas() {
+  const int epts[] = {0, 1, 2, 4, 8};
+  for (int e : epts)
+    LMG_CUDA(cudaFuncSetAttribute(step_cluster_fn<R>(e),
+                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  for (int c : {16, 8, 4, 2}) {
+    cudaLaunchAttribute at[1];
+    const cudaLaunchConfig_t cfg = cluster_config(c, kClusterThreads, nullptr, at);
+    int clusters = 0;
+    bool ok = true;
+    for (int e : epts) {
+      if (cudaOccupancyMaxActiveClusters(&clusters, step_cluster_fn<R>(e), &cfg) != cudaSuccess ||
+          clusters < 1) {
+        ok = false;
+        (void)cudaGetLastError();
+        break;
+      }
+    }
+    if (ok) return c;
+  }
+  return 0;
+}
+
+// One Krylov step as one cluster: elements a thread keeps in registers from
+// the vector length (up to 8 in FP32, 4 in FP64; beyond that streamed).
+template <class R>
+cudaError_t launch_step_cluster(int ctas, int cta_threads, R *w, const R *vi, const R *vprev,
+                                R *vnext, size_t n, int i, KrylovScalars *sc, double *host_ab,
+                                cudaStream_t st) {
+  const size_t threads = (size_t)ctas * cta_threads;
+  const size_t per = (n + threads - 1) / threads;
+  const int max_ept = sizeof(R) == 4 ? 8 : 4;
+  int ept = 0;
+  for (int e : {1, 2, 4, 8})
+    if (ept == 0 && e <= max_ept && per <= (size_t)e) ept = e;
+  cudaLaunchAttribute at[1];
+  const cudaLaunchConfig_t cfg = cluster_config(ctas, cta_threads, st, at);
+  void *args[] = {&w, (void *)&vi, (void *)&vprev, &vnext, &n, &i, &sc, &host_ab};
+  count_launch();
+  return cudaLaunchKernelExC(&cfg, step_cluster_fn<R>(ept), args);
+}
+}  // namespace
+
 // Lanczos to tolerance (LanczosAlgorithm.cu:173-200); returns the iteration
 // index at convergence and leaves y = sqrt(M) z in *y_out.
 //
@@ -621,7 +694,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     rot_cs_.resize(rot_cap);
     rot_idx_.resize(rot_cap);
   }
-  ql_work_.resize(3 * 256);
+  ql_work_.resize(3 * 256 + 18 * 256);  // QL arrays, then the quadrature's work
   RotLog log{rot_cs_.data(), rot_idx_.data(), rot_cap};
   cudaStream_t st = stream();
   cudaStream_t sd = side_;
@@ -636,6 +709,15 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
       throw Error(LMG_ERR_INTERNAL, "[libmobility_gb300] Lanczos step kernel cannot be resident");
   }
   const int step_blocks = std::min(blocks, step_per_sm_ * sms());
+  if (step_ctas_ < 0) step_ctas_ = step_cluster_ctas<R>();
+  const bool step_cluster = g_lanczos_step_mode.load() == 0 && step_ctas_ > 0;
+  // 256-thread CTAs while every thread keeps its elements in registers with
+  // them (measured at n = 12288: 11 us against 17 us with 1024), else 1024
+  // (n = 98304: 20 against 28 us)
+  const int shape = g_lanczos_step_shape.load();
+  const int cl_ctas = shape ? std::min(shape >> 16, step_ctas_) : step_ctas_;
+  const size_t small_n = (size_t)std::max(step_ctas_, 1) * 256 * (sizeof(R) == 4 ? 8 : 4);
+  const int cl_threads = shape ? (shape & 0xffff) : (n <= small_n ? 256 : kClusterThreads);
   double *err_flag = mir_dev + 516;
   mir[516] = 0.0;
   // the tickets and barrier words return to zero after every reduction and
@@ -668,11 +750,16 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     R *vnext = vj + n;
     size_t nn = n;
     int jj = j;
-    void *args[] = {&w, (void *)&vj, (void *)&vprev, &vnext, &nn, &jj, &rp, &tk, &bar,
-                    &sc, &mir_dev, &err_flag};
-    LMG_CUDA(cudaLaunchCooperativeKernel((const void *)krylov_step_kernel<R>, dim3(step_blocks),
-                                         dim3(kRedThreads), args, 0, st));
-    count_launch();
+    if (step_cluster) {
+      LMG_CUDA(launch_step_cluster<R>(cl_ctas, cl_threads, w, vj, vprev, vnext, nn, jj, sc,
+                                      mir_dev, st));
+    } else {
+      void *args[] = {&w, (void *)&vj, (void *)&vprev, &vnext, &nn, &jj, &rp, &tk, &bar,
+                      &sc, &mir_dev, &err_flag};
+      LMG_CUDA(cudaLaunchCooperativeKernel((const void *)krylov_step_kernel<R>,
+                                           dim3(step_blocks), dim3(kRedThreads), args, 0, st));
+      count_launch();
+    }
     if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * j + 2], st));
     LMG_CUDA(cudaEventRecord(ev_iter_[j % kIterEvents], st));
     issued = j + 1;
@@ -695,30 +782,28 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     const int m = i + 1;
     double *cd = cdev + (i & 1) * kMaxLanczosIterations;
     R *yi = yb + (size_t)(i & 1) * n;
-    // estimate y = |z| V c and its error against the previous estimate, on
-    // the side stream once c is in device memory
-    auto estimate_and_error = [&]() {
-      krylov_estimate_kernel<R><<<blocks, kRedThreads, 0, sd>>>(V, n, m, cd, sc, yi, n);
+    // estimate y = |z| V c and its error against the previous estimate, one
+    // launch on the side stream (c in device memory or mapped host memory)
+    auto estimate_and_error = [&](const double *c_dev) {
+      krylov_check_kernel<R><<<blocks, kRedThreads, 0, sd>>>(
+          V, n, m, c_dev, sc, yi, have_prev ? yb + (size_t)((i + 1) & 1) * n : nullptr, n,
+          rp_side, tk_side, mir_dev + 512);
       count_launch();
-      if (have_prev) {
-        krylov_error_kernel<R><<<blocks, kRedThreads, 0, sd>>>(
-            yi, yb + (size_t)((i + 1) & 1) * n, n, rp_side, tk_side, sc, mir_dev + 512);
-        count_launch();
-      }
       if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 4], sd));
       LMG_CUDA(cudaEventRecord(ev_check_, sd));
       LMG_CUDA(cudaGetLastError());
       LMG_CUDA(cudaEventSynchronize(ev_check_));
     };
     NvtxRange nvtx_check("lmg Lanczos check");
-    bool on_host = g_lanczos_device_sqrt.load() == 0;
+    const int sqrt_mode = g_lanczos_device_sqrt.load();
+    bool on_host = sqrt_mode != 1;
     if (!on_host) {
       // c = T^{1/2} e1 by quadrature on the device, right after iteration i
       LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i % kIterEvents], 0));
       if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
       tridiag_sqrt_quad_kernel<<<1, kQuadThreads, 0, sd>>>(sc, m, cd, quad_g, mir_dev + 520);
       count_launch();
-      estimate_and_error();
+      estimate_and_error(cd);
       if (mir[516] != 0.0)
         throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
       on_host = mir[520] != 0.0;  // not positive definite or too ill-conditioned
@@ -733,14 +818,19 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
         be[q] = mir[2 * q + 1];
       }
       double *c = hc + (i & 1) * kMaxLanczosIterations;
-      const int rc = tridiag_sqrt_e1(al.data(), be.data(), m, ql_work_.data(),
-                                     ql_work_.data() + 256, ql_work_.data() + 512, log, c);
+      int rc = 1;
+      if (sqrt_mode == 2)
+        rc = tridiag_sqrt_e1_quad(al.data(), be.data(), m, ql_work_.data() + 768, c);
+      if (rc != 0)
+        rc = tridiag_sqrt_e1(al.data(), be.data(), m, ql_work_.data(), ql_work_.data() + 256,
+                             ql_work_.data() + 512, log, c);
       if (rc != 0)
         for (int q = 0; q < m; q++) c[q] = std::nan("");
+      // c is read by the kernel from mapped host memory: this slot is not
+      // written again before the check two later, after this one completed
       LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i % kIterEvents], 0));
       if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
-      LMG_CUDA(cudaMemcpyAsync(cd, c, m * sizeof(double), cudaMemcpyHostToDevice, sd));
-      estimate_and_error();
+      estimate_and_error(hc_.device_ptr() + (i & 1) * kMaxLanczosIterations);
     }
     if (timing_) checked.push_back(i);
     err = have_prev ? mir[512] : HUGE_VAL;

@@ -252,9 +252,10 @@ def test_nan_in_noise_reports_and_handle_stays_usable(cuda, precision):
 @pytest.mark.parametrize("precision", ["float", "double"])
 @pytest.mark.parametrize("wall", [0, 1])
 def test_device_and_host_square_roots_agree(cuda, precision, wall):
-    """T^{1/2} e1 at the convergence checks by the exact QL on the host (the
-    default) or by quadrature on the device: the same stopping step and the
-    same result (FP64 within 1e-12, FP32 within 1e-6), on fresh handles."""
+    """T^{1/2} e1 at the convergence checks by quadrature on the host (the
+    default), by the exact QL on the host, or by quadrature on the device:
+    the same stopping step and the same result (FP64 within 1e-12, FP32
+    within 1e-6), on fresh handles."""
     from libmobility_gb300 import _capi
     lib = _capi.load()
     rng = np.random.default_rng(90 + wall)
@@ -265,18 +266,19 @@ def test_device_and_host_square_roots_agree(cuda, precision, wall):
     zs = [rng.normal(size=3 * N) for _ in range(3)]
     out = {}
     try:
-        for dev in (1, 0):
-            assert lib.lmg_internal_lanczos_device_sqrt(dev) == 0
+        for mode in (1, 0, 2):
+            assert lib.lmg_internal_lanczos_device_sqrt(mode) == 0
             s = make_solver(wall, 0, 1.0, 1 / (6 * np.pi), precision)
             s.setPositions(p)
-            out[dev] = [s.sqrtMdotW_noise(z) for z in zs]
+            out[mode] = [s.sqrtMdotW_noise(z) for z in zs]
     finally:
-        lib.lmg_internal_lanczos_device_sqrt(0)
+        lib.lmg_internal_lanczos_device_sqrt(2)
     tol = 1e-12 if precision == "double" else 1e-6
-    for (u1, _, it1, _), (u0, _, it0, _) in zip(out[1], out[0]):
-        assert it1 == it0
-        u1, u0 = np.asarray(u1, np.float64), np.asarray(u0, np.float64)
-        assert np.abs(u1 - u0).max() <= tol * np.abs(u0).max()
+    for mode in (1, 2):
+        for (u1, _, it1, _), (u0, _, it0, _) in zip(out[mode], out[0]):
+            assert it1 == it0
+            u1, u0 = np.asarray(u1, np.float64), np.asarray(u0, np.float64)
+            assert np.abs(u1 - u0).max() <= tol * np.abs(u0).max()
 
 
 @pytest.mark.parametrize("precision", ["float", "double"])
@@ -302,3 +304,65 @@ def test_lookahead_changes_nothing(cuda, precision):
     for (u1, _, it1, r1), (u3, _, it3, r3) in zip(out[1], out[3]):
         assert it1 == it3 and r1 == r3
         assert np.array_equal(np.asarray(u1), np.asarray(u3))
+
+
+@pytest.mark.parametrize("precision,wall,ang,N", [
+    ("float", 0, 0, 300),      # one element a thread or none (registers)
+    ("float", 0, 0, 4096),     # configuration 1's size
+    ("float", 1, 1, 8000),     # 48000 elements: four a thread
+    ("float", 0, 0, 40000),    # eight a thread
+    ("float", 0, 0, 60000),    # streamed through memory
+    ("double", 1, 1, 6000),    # FP64, four a thread
+    ("double", 0, 0, 22000),   # FP64, streamed
+])
+def test_cluster_and_grid_steps_agree(cuda, precision, wall, ang, N):
+    """The Lanczos vector step as one thread-block cluster (the default) and
+    as the cooperative grid-wide launch: the same per-element arithmetic,
+    inner products summed in another order (and in double-float instead of
+    FP64 for FP32 vectors), for vector lengths that take each register path
+    of the cluster kernel and the streamed one.
+
+    In FP32 the FP64 scalars agree far below FP32 rounding, so the vectors
+    and results come out bitwise equal.  In FP64 the differences of the
+    scalars (1e-16) reach the vectors, and Lanczos without
+    reorthogonalisation amplifies them once the basis loses orthogonality
+    (measured on these systems: successive-iterate errors equal to 1e-13 over
+    the first 12 iterations, results 4e-4 apart after 23 at tolerance 1e-3).
+    So the check is: the same stopping step, the errors of the first 8
+    iterations (reported by a callback) within 1e-9 relative, the results
+    within 2 x tol.  A wrong element or a lost partial shows in the first
+    errors."""
+    from libmobility_gb300 import _capi
+    lib = _capi.load()
+    rng = np.random.default_rng(N + 7 * wall)
+    side = int(np.ceil(N ** (1 / 3)))
+    g = np.stack(np.meshgrid(*(np.arange(side),) * 3, indexing="ij"), -1).reshape(-1, 3)[:N]
+    p = 3.0 * g + rng.uniform(-0.4, 0.4, (N, 3))
+    if wall:
+        p[:, 2] += 1.5
+    zs = [rng.normal(size=(6 if ang else 3) * N) for _ in range(2)]
+    tol = 1e-3
+    out = {}
+    try:
+        for mode in (0, 1):
+            assert lib.lmg_internal_lanczos_step_mode(mode) == 0
+            errs = []
+            s = make_solver(wall, ang, 1.0, 1 / (6 * np.pi), precision)
+            s.initialize(viscosity=1 / (6 * np.pi), hydrodynamicRadius=1.0,
+                         includeAngular=bool(ang), tolerance=tol,
+                         lanczos_callback=lambda i, e, errs=errs: errs.append(e))
+            s.setPositions(p)
+            out[mode] = ([s.sqrtMdotW_noise(z) for z in zs], errs)
+    finally:
+        lib.lmg_internal_lanczos_step_mode(0)
+    (res0, errs0), (res1, errs1) = out[0], out[1]
+    n8 = min(8, len(errs1))
+    assert np.allclose(errs0[:n8], errs1[:n8], rtol=1e-9, atol=0)
+    for (u1, w1, it1, _), (u0, w0, it0, _) in zip(res0, res1):
+        assert it1 == it0
+        for a, b in ((u1, u0), (w1, w0)) if ang else ((u1, u0),):
+            a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+            if precision == "float":
+                assert np.array_equal(a, b)
+            else:
+                assert np.abs(a - b).max() <= 2 * tol * np.abs(b).max()
