@@ -39,7 +39,8 @@ struct SymArgs {
   unsigned long long *bar;
   int *err;
   // optional timeline (nanoseconds, %globaltimer): per warp [start, end of
-  // its steps], then per block [after the barrier, end of the fold]
+  // its steps], then per block [after the barrier, end of the fold], then
+  // per block the SM it ran on
   unsigned long long *trace;
 };
 
@@ -435,7 +436,12 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
     return;
   }
   const size_t tb = 2 * (size_t)gridDim.x * (kSymThreads / 32) + 2 * blockIdx.x;
-  if (a.trace && threadIdx.x == 0) a.trace[tb] = global_ns();
+  if (a.trace && threadIdx.x == 0) {
+    a.trace[tb] = global_ns();
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    a.trace[2 * (size_t)gridDim.x * (kSymThreads / 32) + 2 * gridDim.x + blockIdx.x] = smid;
+  }
   // two elements per thread and pass, sixteen loads of each in flight
   const int rt = 1 << a.lg_rt;
   const unsigned total = (unsigned)a.ntiles * kElems * rt;

@@ -241,6 +241,10 @@ int lmg_internal_lanczos_step_shape(int ctas, int threads) {
   return 0;
 }
 
+// Timeline of the symmetric kernel's next launches (null: off): buf is a
+// device array of at least 2 x warps + 3 x blocks 64-bit values of the
+// launch's grid (per warp its start and end in %globaltimer nanoseconds, per
+// block the end of its barrier wait and of its fold, per block its SM).
 int lmg_internal_sym_trace(void *buf) {
   lmg::g_sym_trace.store(static_cast<unsigned long long *>(buf));
   return 0;
