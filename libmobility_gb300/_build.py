@@ -29,6 +29,7 @@ UNITS = [
     ("probes.cu", [], "probes.o"),
     ("noalloc.cu", [], "noalloc.o"),
     ("precond.cu", [], "precond.o"),
+    ("tc_gemm.cu", [], "tc_gemm.o"),
     ("ensemble.cu", [], "ensemble.o"),
     ("solver_base.cpp", [], "solver_base.o"),
     ("capi.cpp", [], "capi.o"),

@@ -110,6 +110,9 @@ def load():
     internal = {
         "lmg_internal_gemm": [_I, _I, _I, _I, _I, _VP, _I, _VP, _I, _VP, _I, _VP, _I, _F, _VP],
         "lmg_internal_tanh_backward": [_SZ, _VP, _VP, _VP],
+        "lmg_internal_tc_gemm": [_I, _I, _I, _VP, _I, _VP, _I, _VP, _I, _VP, _I, _VP],
+        "lmg_internal_tc_status": [_I],
+        "lmg_internal_precond_tc": [_I],
         "lmg_internal_mse_grad": [_SZ, _VP, _VP, _VP, _F, _VP, _VP],
         "lmg_internal_colsum": [_I, _I, _VP, _VP, _VP],
         "lmg_internal_adam": [_SZ, _VP, _VP, _VP, _VP, _F, _F, _F, _F, _I, _VP],

@@ -25,6 +25,9 @@ extern std::atomic<int> g_lanczos_step_mode;
 // its cluster shape, (CTAs << 16) | threads per CTA (0 = the largest cluster
 // of kClusterThreads-thread CTAs that fits)
 extern std::atomic<int> g_lanczos_step_shape;
+// network layers of the preconditioner build on the tensor cores (tcgen05,
+// TF32): 1 on, 0 the CUDA-core FP32 GEMM
+extern std::atomic<int> g_precond_tc;
 // device buffer for the symmetric kernel's timeline (null = off)
 extern std::atomic<unsigned long long *> g_sym_trace;
 }  // namespace lmg

@@ -12,6 +12,7 @@
 
 #include "launch_count.hpp"
 #include "precond.cuh"
+#include "tc_gemm.cuh"
 
 namespace lmg {
 
@@ -296,7 +297,7 @@ template <int K, bool WALL>
 __global__ void __launch_bounds__(kBuildThreads)
 precond_features_kernel(const float *__restrict__ pos, const int *__restrict__ nb, int N,
                         const float *__restrict__ xmean, const float *__restrict__ xstd,
-                        float inv_a, float *__restrict__ X, float *__restrict__ E) {
+                        float inv_a, float *__restrict__ X, int ldx, float *__restrict__ E) {
   constexpr int In = 3 * K + (WALL ? 1 : 0);
   const int i = blockIdx.x * kBuildThreads + threadIdx.x;
   if (i >= N) return;
@@ -362,7 +363,7 @@ precond_features_kernel(const float *__restrict__ pos, const int *__restrict__ n
     e[2][1] = e[0][2] * y0 - e[0][0] * y2;
     e[2][2] = e[0][0] * y1 - e[0][1] * y0;
   }
-  float *x = X + (size_t)i * In;
+  float *x = X + (size_t)i * ldx;
 #pragma unroll
   for (int n = 0; n < K; n++) {
 #pragma unroll
@@ -435,6 +436,30 @@ cudaError_t gemm_launch(int ta, int tb, int M, int N, int K, const float *A, int
                         const float *B, int ldb, float *C, int ldc, const float *bias, int act,
                         float beta, cudaStream_t s);
 
+// out[c][r] = in[r][c] (in: rows x cols, row-major; out rows ldo apart)
+__global__ void transpose_kernel(const float *__restrict__ in, int rows, int cols,
+                                 float *__restrict__ out, int ldo) {
+  __shared__ float t[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int r = r0 + k, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) t[k][threadIdx.x] = in[(size_t)r * cols + c];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int c = c0 + k, r = r0 + threadIdx.x;
+    if (c < cols && r < rows) out[(size_t)c * ldo + r] = t[threadIdx.x][k];
+  }
+}
+
+cudaError_t transpose_launch(const float *in, int rows, int cols, float *out, int ldo,
+                             cudaStream_t s) {
+  count_launch();
+  transpose_kernel<<<dim3((cols + 31) / 32, (rows + 31) / 32), dim3(32, 8), 0, s>>>(in, rows, cols,
+                                                                                    out, ldo);
+  return cudaGetLastError();
+}
+
 cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const int *nb, int N,
                                  const float *params, float inv_a, float scale, void *blocks,
                                  bool half, PrecWork *work, cudaStream_t stream) {
@@ -442,7 +467,10 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
   if (N <= 0) return cudaSuccess;
   PrecWork local;
   PrecWork &w = work ? *work : local;
-  float *X = w.X.ensure((size_t)N * L.In);
+  // the tensor-core GEMM takes rows of a multiple of 4 floats (16 bytes)
+  const bool tc = g_precond_tc.load() != 0 && tc_gemm_available();
+  const int ldx = tc ? (L.In + 3) & ~3 : L.In;
+  float *X = w.X.ensure((size_t)N * ldx);
   float *E = w.E.ensure((size_t)N * 9);
   float *H1 = w.H1.ensure((size_t)N * L.H);
   float *H2 = w.H2.ensure((size_t)N * L.H);
@@ -454,10 +482,10 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
   if (L.K == KK) {                                                                         \
     if (L.wall)                                                                            \
       precond_features_kernel<KK, true><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm, xs, \
-                                                                         inv_a, X, E);     \
+                                                                         inv_a, X, ldx, E); \
     else                                                                                   \
-      precond_features_kernel<KK, false><<<g, kBuildThreads, 0, stream>>>(pos, nb, N, xm,   \
-                                                                          xs, inv_a, X, E); \
+      precond_features_kernel<KK, false><<<g, kBuildThreads, 0, stream>>>(               \
+          pos, nb, N, xm, xs, inv_a, X, ldx, E);                                           \
   }
   LMG_FEATURES(16)
   LMG_FEATURES(32)
@@ -465,15 +493,31 @@ cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const in
   LMG_FEATURES(64)
 #undef LMG_FEATURES
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess)
-    e = gemm_launch(0, 0, N, L.H, L.In, X, L.In, params + L.W1, L.H, H1, L.H, params + L.B1, 1,
-                    0.f, stream);
-  if (e == cudaSuccess)
-    e = gemm_launch(0, 0, N, L.H, L.H, H1, L.H, params + L.W2, L.H, H2, L.H, params + L.B2, 1,
-                    0.f, stream);
-  if (e == cudaSuccess)
-    e = gemm_launch(0, 0, N, L.Out, L.H, H2, L.H, params + L.W3, L.Out, Y, L.Out,
-                    params + L.B3, 0, 0.f, stream);
+  if (tc) {
+    // tcgen05 (TF32) layers: the weights transposed to K-major rows first
+    const int ld1 = (L.In + 3) & ~3;
+    float *WT = w.WT.ensure((size_t)L.H * ld1 + (size_t)L.H * L.H + (size_t)L.Out * L.H);
+    float *WT1 = WT, *WT2 = WT1 + (size_t)L.H * ld1, *WT3 = WT2 + (size_t)L.H * L.H;
+    if (e == cudaSuccess) e = transpose_launch(params + L.W1, L.In, L.H, WT1, ld1, stream);
+    if (e == cudaSuccess) e = transpose_launch(params + L.W2, L.H, L.H, WT2, L.H, stream);
+    if (e == cudaSuccess) e = transpose_launch(params + L.W3, L.H, L.Out, WT3, L.H, stream);
+    if (e == cudaSuccess)
+      e = tc_gemm_launch(N, L.H, L.In, X, ldx, WT1, ld1, H1, L.H, params + L.B1, 1, stream);
+    if (e == cudaSuccess)
+      e = tc_gemm_launch(N, L.H, L.H, H1, L.H, WT2, L.H, H2, L.H, params + L.B2, 1, stream);
+    if (e == cudaSuccess)
+      e = tc_gemm_launch(N, L.Out, L.H, H2, L.H, WT3, L.H, Y, L.Out, params + L.B3, 0, stream);
+  } else {
+    if (e == cudaSuccess)
+      e = gemm_launch(0, 0, N, L.H, L.In, X, L.In, params + L.W1, L.H, H1, L.H, params + L.B1,
+                      1, 0.f, stream);
+    if (e == cudaSuccess)
+      e = gemm_launch(0, 0, N, L.H, L.H, H1, L.H, params + L.W2, L.H, H2, L.H, params + L.B2,
+                      1, 0.f, stream);
+    if (e == cudaSuccess)
+      e = gemm_launch(0, 0, N, L.Out, L.H, H2, L.H, params + L.W3, L.Out, Y, L.Out,
+                      params + L.B3, 0, 0.f, stream);
+  }
   if (e != cudaSuccess) return e;
   const long nblk = (long)N * (L.K + 1);
   const int ga = (int)((nblk + 255) / 256);
@@ -824,6 +868,25 @@ int lmg_internal_gemm(int ta, int tb, int M, int N, int K, const float *A, int l
                       float beta, void *stream) {
   return (int)lmg::gemm_launch(ta, tb, M, N, K, A, lda, B, ldb, C, ldc, bias, act, beta,
                                (cudaStream_t)stream);
+}
+
+// C = act(A Bt^T + bias) on the tensor cores (tcgen05, TF32); see tc_gemm.cuh.
+int lmg_internal_tc_gemm(int M, int N, int K, const float *A, int lda, const float *Bt, int ldbt,
+                         float *C, int ldc, const float *bias, int act, void *stream) {
+  return (int)lmg::tc_gemm_launch(M, N, K, A, lda, Bt, ldbt, C, ldc, bias, act,
+                                  (cudaStream_t)stream);
+}
+
+// Status word of the tensor-core GEMM (non-zero: a bounded wait ran out);
+// reset != 0 clears it.  -1 if it cannot be read.
+int lmg_internal_tc_status(int reset) { return lmg::tc_gemm_status(reset != 0); }
+
+// 1: the preconditioner build runs its network on the tensor cores where the
+// GPU has them; 0: on the CUDA cores.  Returns 1 for a bad value.
+int lmg_internal_precond_tc(int on) {
+  if (on != 0 && on != 1) return 1;
+  lmg::g_precond_tc.store(on);
+  return 0;
 }
 
 int lmg_internal_tanh_backward(size_t n, const float *h, float *g, void *stream) {

@@ -99,11 +99,13 @@ cudaError_t knn_launch(int K, const float *pos, int N, int nper, int *nb, cudaSt
 // activations H1, H2 [N][H], network outputs Y [N][6+9K].
 struct PrecWork {
   DeviceBuffer<float> X, E, H1, H2, Y;
+  DeviceBuffer<float> WT;  // weights transposed for the tensor-core layers
 };
 // P blocks from positions and neighbour lists: features and canonical frames
 // (one thread per particle), the three layers as GEMMs of all particles at
-// once (this library's GEMM kernel, bias and tanh fused), then the blocks
-// rotated back to the lab frame and scaled.
+// once (bias and tanh fused: the tcgen05 TF32 kernel of tc_gemm.cu where the
+// GPU has it and it is switched on, else this library's CUDA-core GEMM),
+// then the blocks rotated back to the lab frame and scaled.
 cudaError_t precond_build_launch(const PrecLayout &L, const float *pos, const int *nb, int N,
                                  const float *params, float inv_a, float scale, void *blocks,
                                  bool half, PrecWork *work, cudaStream_t stream);

@@ -25,6 +25,7 @@ std::atomic<int> g_sym_mode{0}, g_sym_warps{0}, g_sym_variant{0};
 std::atomic<unsigned long long *> g_sym_trace{nullptr};
 std::atomic<int> g_lanczos_device_sqrt{2};
 std::atomic<int> g_lanczos_lookahead{0};
+std::atomic<int> g_precond_tc{0};
 std::atomic<int> g_lanczos_step_mode{0};
 std::atomic<int> g_lanczos_step_shape{0};
 }
