@@ -21,6 +21,7 @@ With --gpus N > 1 (under torchrun) every rank runs its own replica of the
 workload on its own GPU; there is no collective on the data path.
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -523,6 +524,79 @@ def sqrtmdotw_comparison(torch, steps, warmup, rank, N=65536):
     return out
 
 
+def precond_network_gemms(torch, lib, M=65536):
+    """The preconditioner network's three layers (the shipped open network:
+    48 neighbours, 512-512 hidden units, 438 outputs) as GEMMs over M = 65536
+    particles, on the tensor cores (tcgen05 kind::tf32, TMA-fed, accumulator
+    in tensor memory) and on the CUDA cores (FP32, the build's default),
+    CUDA-event timed on device buffers; then the whole build both ways.  The
+    tensor-core figures are against the bf16 cuBLAS peak halved (TF32 runs at
+    half the bf16 rate)."""
+    from libmobility_gb300 import precond as pc
+    p = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def ev(fn, reps=10):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps * 1e-3
+
+    st = lambda: ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)  # noqa: E731
+    peak = None
+    try:
+        with open(Path(__file__).resolve().parent / "MEASURED_PEAKS.json") as f:
+            peak = json.load(f)["bf16_tflops"] / 2
+    except Exception:
+        pass
+    out = {"M": M, "tf32_peak_tflops": peak,
+           "peak_source": "MEASURED_PEAKS.json bf16_tflops / 2 (TF32 rate)"}
+    g = torch.Generator(device="cuda").manual_seed(5)
+    layers = []
+    for (N, K) in ((512, 144), (512, 512), (438, 512)):
+        A = torch.randn(M, K, generator=g, device="cuda")
+        Bt = torch.randn(N, K, generator=g, device="cuda") / math.sqrt(K)
+        B = Bt.t().contiguous()
+        bias = torch.randn(N, generator=g, device="cuda")
+        C1 = torch.empty(M, N, device="cuda")
+        C2 = torch.empty(M, N, device="cuda")
+        t_tc = ev(lambda: lib.lmg_internal_tc_gemm(M, N, K, p(A), K, p(Bt), K, p(C1), N, p(bias),
+                                                   1, st()))
+        t_cc = ev(lambda: lib.lmg_internal_gemm(0, 0, M, N, K, p(A), K, p(B), N, p(C2), N,
+                                                p(bias), 1, ctypes.c_float(0.0), st()))
+        fl = 2.0 * M * N * K
+        ach = fl / t_tc / 1e12
+        layers.append({"N": N, "K": K, "tensor_core_us": t_tc * 1e6, "cuda_core_us": t_cc * 1e6,
+                       "tensor_core_tflops": ach, "cuda_core_tflops": fl / t_cc / 1e12,
+                       "frac_of_tf32_peak": ach / peak if peak else None,
+                       "max_abs_diff": float((C1 - C2).abs().max())})
+    out["layers"] = layers
+    out["tc_status"] = lib.lmg_internal_tc_status(1)
+    params = pc.load_weights(pc.default_weights(False))
+    k, h = pc.shape_of_params(len(params))
+    rng = np.random.default_rng(3)
+    L = (M * 4 * math.pi / 3 / 0.2) ** (1 / 3)
+    pos = torch.tensor(rng.uniform(0, L, (M, 3)), dtype=torch.float32, device="cuda")
+    dparams = torch.tensor(params, device="cuda")
+    nb = torch.empty((k + 1, M), dtype=torch.int32, device="cuda")
+    lib.lmg_internal_knn_k(k, p(pos), M, M, p(nb), None)
+    blk = torch.empty((k + 1, 9, M), device="cuda")
+    try:
+        for name, tc in (("build_cuda_core_ms", 0), ("build_tensor_core_ms", 1)):
+            assert lib.lmg_internal_precond_tc(tc) == 0
+            out[name] = 1e3 * ev(lambda: lib.lmg_internal_precond_build_kh(
+                k, h, p(pos), p(nb), M, p(dparams), 1.0, 1.0, p(blk), st()), reps=5)
+    finally:
+        lib.lmg_internal_precond_tc(0)
+    out["default"] = "cuda_core (the TF32 network adds about 3 Lanczos iterations per solve)"
+    return out
+
+
 def ensemble_systems(rng, nsys=256):
     """256 systems, N ~ U[200, 4000], half open and half single wall,
     volume fraction ~ U[0.02, 0.25] each (a = 1): open systems uniform in a
@@ -922,6 +996,7 @@ def run_ours(args, w, ws, rank, local):
         # the preconditioned stopping step moves by +-4 from one dW to the next:
         # at least 8 solves per arm
         cmp = sqrtmdotw_comparison(torch, max(8, args.steps), 2, rank)
+        cmp["network_gemm"] = precond_network_gemms(torch, lib)
     ens = None
     if not args.skip_ensemble:
         ens = ensemble_comparison(torch, max(2, args.steps), 2, rank)
@@ -993,7 +1068,8 @@ def main():
                     help="skip the N = 262144 single-wall Mdot and square roots")
     ap.add_argument("--skip-reference-gpu", action="store_true",
                     help="skip the reference CUDA kernel timed beside this library's Mdot")
-    ap.add_argument("--only", choices=["ensemble", "precond", "open4k", "large"], default=None,
+    ap.add_argument("--only", choices=["ensemble", "precond", "open4k", "large", "tcgemm"],
+                    default=None,
                     help="run one sub-measurement alone and print it (for profiling)")
     ap.add_argument("--ensemble-systems", type=int, default=256)
     args = ap.parse_args()
@@ -1011,6 +1087,13 @@ def main():
         out = sqrtmdotw_comparison(torch, args.steps, args.warmup, rank)
         if rank == 0:
             print(json.dumps({"sqrtMdotW_learned_vs_plain": out}))
+        return
+    if args.only == "tcgemm":  # the preconditioner network's GEMMs alone (profiling runs)
+        import torch
+        from libmobility_gb300 import _capi
+        out = precond_network_gemms(torch, _capi.load())
+        if rank == 0:
+            print(json.dumps({"precond_network_gemm": out}))
         return
     if args.only == "large":  # configuration 5's square roots alone
         import torch

@@ -10,7 +10,9 @@
 //     columns the CTA allocated; tcgen05.commit frees the stage for its next
 //     load, and a last commit signals the end of the products;
 //   * all four warps then read their 32 tensor-memory lanes (rows) with
-//     tcgen05.ld, add the bias, apply tanh and store C.
+//     tcgen05.ld, add the bias, apply tanh, stage the rows in the idle stage
+//     buffers and write them to C with consecutive lanes on consecutive
+//     columns.
 // Every wait on an mbarrier is bounded (~0.4 s); one that runs out sets a
 // status word, the CTA waits (bounded) for its products and copies in flight,
 // frees its tensor memory and returns without writing C.
@@ -37,6 +39,9 @@ constexpr uint32_t kABytes = kBM * kBK * 4;
 constexpr uint32_t kBBytes = kBN * kBK * 4;
 constexpr uint32_t kStageBytes = kABytes + kBBytes;
 constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024;  // + alignment slack
+constexpr int kPitch = kBN + 4;  // floats per row of the output staging tile
+static_assert((size_t)kBM * kPitch * 4 <= (size_t)kStages * kStageBytes,
+              "the output staging tile reuses the stage buffers");
 constexpr long kSpins = 1L << 22;
 
 __device__ int g_tc_status;
@@ -196,24 +201,35 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   const bool ok = mbar_wait(done, 0);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
-    const int row = m0 + 32 * warp + lane;
+    // tensor memory -> bias, activation -> a row-major staging tile in the
+    // (now idle) stage buffers -> coalesced rows of C
+    float *stage = reinterpret_cast<float *>(smem_raw + (base - smem_u32(smem_raw)));
+    const int r = 32 * warp + lane;  // this thread's row of the tile
     const uint32_t lane_base = tmem + ((uint32_t)(32 * warp) << 16);
-    for (int j = 0; j < kBN && n0 + j < N; j += 16) {
+    const int ncols = min(kBN, N - n0);
+    for (int j = 0; j < ncols; j += 16) {
       uint32_t v[16];
       tmem_ld16(lane_base + (uint32_t)j, v);
-      if (row < M) {
-        float *out = C + (size_t)row * ldc;
+      float x[16];
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-          const int col = n0 + j + q;
-          if (col < N) {
-            float x = __uint_as_float(v[q]);
-            if (bias) x += __ldg(bias + col);
-            if (act == 1) x = tanhf(x);
-            out[col] = x;
-          }
-        }
+      for (int q = 0; q < 16; q++) {
+        x[q] = __uint_as_float(v[q]);
+        const int col = n0 + j + q;
+        if (bias && col < N) x[q] += __ldg(bias + col);
+        if (act == 1) x[q] = tanhf(x[q]);
       }
+      float4 *dst = reinterpret_cast<float4 *>(stage + (size_t)r * kPitch + j);
+#pragma unroll
+      for (int q = 0; q < 4; q++) dst[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+    }
+    __syncwarp();
+    // each warp writes its own 32 rows, a row at a time, lanes on consecutive columns
+    for (int rr = 0; rr < 32; rr++) {
+      const int row = m0 + 32 * warp + rr;
+      if (row >= M) break;
+      const float *src = stage + (size_t)(32 * warp + rr) * kPitch;
+      float *out = C + (size_t)row * ldc + n0;
+      for (int c = lane; c < ncols; c += 32) out[c] = src[c];
     }
   } else if (threadIdx.x == 0) {
     atomicExch(&g_tc_status, 3);
