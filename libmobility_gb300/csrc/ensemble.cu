@@ -54,6 +54,7 @@ namespace {
 constexpr int kPad = 128;            // systems padded to a multiple of this
 constexpr int kEnsThreads = 256;     // threads of the per-system vector kernels
 constexpr int kEnsLimit = 200;       // lanczos::Solver::iterationHardLimit
+constexpr size_t kEnsBranches = 8;   // streams the groups' products run on side by side
 constexpr int kEstChunk = 4 * kEnsThreads;  // elements of one system per estimate CTA
 constexpr double kDummyFar = 1e5;    // dummy particles: radii away from everything
 
@@ -407,6 +408,7 @@ template <class R> class Ensemble final : public EnsembleBase {
   Ensemble() : pool_(pool_threads()) {}
   ~Ensemble() override {
     drop_graph();
+    release_branches();
     if (ev_ready_) {
       cudaEventDestroy(ev_iter_[0]);
       cudaEventDestroy(ev_iter_[1]);
@@ -445,6 +447,10 @@ template <class R> class Ensemble final : public EnsembleBase {
     MdotPlan plan;
     bool tuned = false;
     std::vector<std::pair<int, double>> trials;  // (nsplit, ms)
+    // this group's share of the split scratch, so groups can run at once
+    size_t part_off = 0, ticket_off = 0;
+    double work = 0;  // pair flops of one product (padded sizes)
+    int branch = 0;   // stream it runs on beside the others
   };
 
   cudaStream_t stream() {
@@ -523,8 +529,8 @@ template <class R> class Ensemble final : public EnsembleBase {
     a.inv_a = (R)(1.0 / a_);
     a.k = make_pair_const<R>(t0_, r0_, rt0_);
     a.kw = make_wall_const(t0_, r0_, rt0_);
-    a.part = part_.ptr;
-    a.ticket = tickets_.ptr;
+    a.part = part_.ptr + g.part_off;
+    a.ticket = tickets_.ptr + g.ticket_off;
     a.sys_active = active ? active + g.s0 : nullptr;
     return a;
   }
@@ -538,9 +544,49 @@ template <class R> class Ensemble final : public EnsembleBase {
   void launch_group(Group &g, const R *x, R *y, const int *active, cudaStream_t st) {
     LMG_CUDA(mdot_launch<R>(shape(g), args(g, x, y, active), g.plan, st));
   }
-  void matvec(const R *x, R *y, const int *active) {
-    for (auto &g : groups_) launch_group(*g, x, y, active, stream());
+  // every group's product, the groups side by side on streams forked from
+  // st and joined back into it (their outputs, scratch and tickets are
+  // disjoint), so one group's last wave overlaps the others' work
+  void launch_groups(const R *x, R *y, const int *active, cudaStream_t st) {
+    if (groups_.size() <= 1) {
+      for (auto &g : groups_) launch_group(*g, x, y, active, st);
+      return;
+    }
+    ensure_branches();
+    LMG_CUDA(cudaEventRecord(ev_fork_, st));
+    for (size_t q = 0; q < branch_.size(); q++) LMG_CUDA(cudaStreamWaitEvent(branch_[q], ev_fork_, 0));
+    // the largest products are issued first on their streams
+    std::vector<int> ord(groups_.size());
+    for (size_t q = 0; q < ord.size(); q++) ord[q] = (int)q;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int a, int b) { return groups_[a]->work > groups_[b]->work; });
+    for (int q : ord)
+      launch_group(*groups_[q], x, y, active, branch_[groups_[q]->branch % branch_.size()]);
+    for (size_t q = 0; q < branch_.size() && q < groups_.size(); q++) {
+      LMG_CUDA(cudaEventRecord(ev_join_[q], branch_[q]));
+      LMG_CUDA(cudaStreamWaitEvent(st, ev_join_[q], 0));
+    }
   }
+  void ensure_branches() {
+    if (!branch_.empty()) return;
+    const size_t nb = std::min<size_t>(groups_.size(), kEnsBranches);
+    branch_.resize(nb);
+    ev_join_.resize(nb);
+    for (size_t q = 0; q < nb; q++) {
+      LMG_CUDA(cudaStreamCreateWithFlags(&branch_[q], cudaStreamNonBlocking));
+      LMG_CUDA(cudaEventCreateWithFlags(&ev_join_[q], cudaEventDisableTiming));
+    }
+    LMG_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+  }
+  void release_branches() {
+    for (auto b : branch_) cudaStreamDestroy(b);
+    for (auto e : ev_join_) cudaEventDestroy(e);
+    if (ev_fork_) cudaEventDestroy(ev_fork_);
+    branch_.clear();
+    ev_join_.clear();
+    ev_fork_ = nullptr;
+  }
+  void matvec(const R *x, R *y, const int *active) { launch_groups(x, y, active, stream()); }
   void ensure_plans();
   void build_graph(R *V, size_t ldv);
 
@@ -572,6 +618,10 @@ template <class R> class Ensemble final : public EnsembleBase {
   // the legacy default stream, which cannot be captured); the graph is then
   // launched on the working stream
   cudaStream_t stream_ = nullptr, own_ = nullptr, side_ = nullptr, cap_ = nullptr;
+  // streams the groups' products run on side by side, and their fork / join
+  std::vector<cudaStream_t> branch_;
+  std::vector<cudaEvent_t> ev_join_;
+  cudaEvent_t ev_fork_ = nullptr;
   bool have_stream_ = false, ev_ready_ = false;
   cudaEvent_t ev_iter_[2] = {nullptr, nullptr}, ev_check_ = nullptr, ev_side_ = nullptr;
   cudaEvent_t ev_t0_ = nullptr, ev_t1_ = nullptr;
@@ -644,10 +694,26 @@ void Ensemble<R>::set_systems(int nsys, const int *sizes, const int *geometry,
     g->p1 = ioff_[g->s1];
     std::vector<int> sb(g->s1 - g->s0 + 1);
     for (int k = g->s0; k <= g->s1; k++) sb[k - g->s0] = ioff_[k] - g->p0;
-    for (int k = g->s0; k < g->s1; k++) g->span = std::max(g->span, pad_[k]);
+    for (int k = g->s0; k < g->s1; k++) {
+      g->span = std::max(g->span, pad_[k]);
+      g->work += (double)pad_[k] * pad_[k] * (g->geom ? 160.0 : 36.0);
+    }
     int *d = g->sys_begin.ensure(sb.size());
     LMG_CUDA(cudaMemcpy(d, sb.data(), sb.size() * sizeof(int), cudaMemcpyHostToDevice));
     groups_.push_back(std::move(g));
+  }
+  // branches: the largest products first, each onto the least loaded stream
+  {
+    std::vector<int> ord(groups_.size());
+    for (size_t q = 0; q < ord.size(); q++) ord[q] = (int)q;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int a, int b) { return groups_[a]->work > groups_[b]->work; });
+    std::vector<double> load(std::min<size_t>(groups_.size(), kEnsBranches), 0.0);
+    for (int q : ord) {
+      const size_t b = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
+      groups_[q]->branch = (int)b;
+      load[b] += groups_[q]->work;
+    }
   }
   // per internal particle: caller's particle index (-1 for dummies), system
   std::vector<int> imap(npad_, -1), psys(npad_), sgeom(nsys), off3(nsys), nn(nsys);
@@ -792,6 +858,18 @@ template <class R> void Ensemble<R>::ensure_plans() {
     ensure_scratch(g.plan);
     g.tuned = true;
   }
+  // disjoint scratch per group (the tuning above ran the groups one at a time
+  // on the start of the buffers); new tickets start at zero
+  size_t part = 0, tick = 0;
+  for (auto &gp : groups_) {
+    gp->part_off = part;
+    gp->ticket_off = tick;
+    part += gp->plan.part_elems;
+    tick += gp->plan.tickets;
+  }
+  part_.ensure(std::max<size_t>(part, 1));
+  if (tickets_.count < std::max<size_t>(tick, 1)) tickets_.ensure(std::max<size_t>(tick, 1));
+  LMG_CUDA(cudaMemsetAsync(tickets_.ptr, 0, tickets_.count * sizeof(unsigned), st));
   drop_graph();
 }
 
@@ -811,7 +889,7 @@ template <class R> void Ensemble<R>::build_graph(R *V, size_t ldv) {
   cudaGraph_t g = nullptr;
   LMG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   try {
-    for (auto &gp : groups_) launch_group(*gp, vcur_.ptr, w_.ptr, active_.ptr, st);
+    launch_groups(vcur_.ptr, w_.ptr, active_.ptr, st);
     const dim3 cg(nsys_, est_chunks_);
     ens_step_alpha<R><<<cg, kEnsThreads, 0, st>>>(w_.ptr, V, ldv, iter_.ptr, off3_.ptr, nn_.ptr,
                                                   active_.ptr, beta_.ptr, alpha_.ptr, kEnsLimit,
