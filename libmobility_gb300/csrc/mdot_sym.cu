@@ -22,6 +22,7 @@ constexpr long long kSymMinSteps = 4;
 // line far from the origin (their own sums are never read).
 constexpr float kPadX = 1.0e6f;
 constexpr int kElems = 3 * kSymTile;  // floats of one partial slot
+constexpr int kFoldH = 3;              // output elements a thread folds per pass
 
 struct SymArgs {
   const float *pos;
@@ -442,18 +443,21 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
     a.trace[2 * (size_t)gridDim.x * (kSymThreads / 32) + 2 * gridDim.x + blockIdx.x] = smid;
   }
-  // two elements per thread and pass, sixteen loads of each in flight
+  // kFoldH elements per thread and pass, sixteen loads of each in flight (at
+  // N = 4096 one pass covers every element)
   const int rt = 1 << a.lg_rt;
   const unsigned total = (unsigned)a.ntiles * kElems * rt;
   const unsigned stride = gridDim.x * blockDim.x;
   for (unsigned base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
-       base += 2 * stride) {
-    float S[2] = {0.f, 0.f}, C[2] = {0.f, 0.f};
-    int t[2], e[2], sub[2], cnt[2];
-    bool in[2];
-    const float *src[2];
+       base += kFoldH * stride) {
+    float S[kFoldH], C[kFoldH];
+    int t[kFoldH], e[kFoldH], sub[kFoldH], cnt[kFoldH];
+    bool in[kFoldH];
+    const float *src[kFoldH];
+    int cmx = 0;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < kFoldH; h++) {
+      S[h] = C[h] = 0.f;
       const unsigned g = base + h * stride + lane;
       in[h] = g < total;
       const unsigned el = in[h] ? g >> a.lg_rt : 0u;
@@ -462,12 +466,13 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
       e[h] = (int)(el - (unsigned)t[h] * kElems);
       src[h] = a.part + (size_t)t[h] * a.cmax * kElems + e[h];
       cnt[h] = in[h] ? a.cmax : 0;
+      cmx = max(cmx, cnt[h]);
     }
     // each tile's slot range, in slot order (share `sub` of every rt)
-    for (int m0 = 0; m0 < max(cnt[0], cnt[1]); m0 += 16 * rt) {
-      float v[2][16];
+    for (int m0 = 0; m0 < cmx; m0 += 16 * rt) {
+      float v[kFoldH][16];
 #pragma unroll
-      for (int h = 0; h < 2; h++)
+      for (int h = 0; h < kFoldH; h++)
 #pragma unroll
         for (int m = 0; m < 16; m++) {
           const int j = m0 + sub[h] + m * rt;
@@ -477,12 +482,12 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
                         ? __ldcg(src[h] + (size_t)j * kElems) : 0.f;
         }
 #pragma unroll
-      for (int h = 0; h < 2; h++)
+      for (int h = 0; h < kFoldH; h++)
 #pragma unroll
         for (int m = 0; m < 16; m++) fold(S[h], C[h], v[h][m]);
     }
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < kFoldH; h++) {
       // combine the rt shares (the same value lands in every lane of a group)
       for (int o = 1; o < rt; o <<= 1) {
         const float S2 = __shfl_xor_sync(0xffffffffu, S[h], o);
