@@ -883,8 +883,10 @@ tridiag_sqrt_quad_kernel(const KrylovScalars *sc, int m, double *out, double *G,
 // yprev| / |yprev| (FP64) -> sc->err and the mapped host copy: the estimate
 // and the error of one convergence check in one launch (each thread's
 // elements of y feed its share of the error sums directly).  V is row-major
-// (row k is v_k, ldv elements apart); c may live in mapped host memory.
-template <class R>
+// (row k is v_k, ldv elements apart); c may live in mapped host memory.  For
+// short vectors (TPE = 4) each element's sum over the basis is shared by four
+// threads, so a check is not a chain of m dependent loads.
+template <class R, int TPE>
 __global__ void krylov_check_kernel(const R *V, size_t ldv, int m, const double *c,
                                     KrylovScalars *sc, R *y, const R *yprev, size_t n,
                                     double *partials, unsigned *ticket, double *host_err) {
@@ -892,16 +894,29 @@ __global__ void krylov_check_kernel(const R *V, size_t ldv, int m, const double 
   const double nz = sc->normz;
   for (int k = threadIdx.x; k < m; k += blockDim.x) cs[k] = (R)(nz * c[k]);
   __syncthreads();
+  // TPE consecutive threads share an element, thread `part` taking the basis
+  // vectors k = part, part + TPE, ...; their sums meet in a fixed xor tree.
+  // The pass loop is the same for every thread (the shuffles need the whole
+  // warp), elements past n contribute nothing.
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const int part = (int)(tid % TPE);
+  const size_t per_pass = (size_t)gridDim.x * blockDim.x / TPE;
   double v[2] = {0.0, 0.0};
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x) {
+  for (size_t e0 = 0; e0 < n; e0 += per_pass) {
+    const size_t e = e0 + tid / TPE;
+    const bool ok = e < n;
     R acc = 0;
-    for (int k = 0; k < m; k++) acc += cs[k] * V[(size_t)k * ldv + e];
-    y[e] = acc;
-    if (yprev) {
-      const double a = (double)yprev[e], dlt = (double)acc - a;
-      v[0] += a * a;
-      v[1] += dlt * dlt;
+    if (ok)
+      for (int k = part; k < m; k += TPE) acc += cs[k] * V[(size_t)k * ldv + e];
+#pragma unroll
+    for (int o = 1; o < TPE; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (ok && part == 0) {
+      y[e] = acc;
+      if (yprev) {
+        const double a = (double)yprev[e], dlt = (double)acc - a;
+        v[0] += a * a;
+        v[1] += dlt * dlt;
+      }
     }
   }
   if (!yprev) return;

@@ -578,6 +578,9 @@ template <class R> void Solver<R>::ensure_side() {
 }
 
 namespace {
+// vectors up to this length take the check kernel with four threads per element
+constexpr size_t kCheckShortN = 65536;
+
 template <class R> const void *step_cluster_fn(int ept) {
   switch (ept) {
     case 1: return (const void *)krylov_step_cluster_kernel<R, 1>;
@@ -700,7 +703,6 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
   cudaStream_t sd = side_;
   unsigned *tk = red_ticket_.ptr, *tk_side = red_ticket_.ptr + 1, *bar = red_ticket_.ptr + 4;
   double *rp = red_part_.ptr, *rp_side = red_part_.ptr + red_half();
-  const size_t n3 = 3 * (size_t)N_;
   // the fused vector step is a cooperative launch: every block resident
   if (!step_per_sm_) {
     LMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&step_per_sm_, krylov_step_kernel<R>,
@@ -785,9 +787,13 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     // estimate y = |z| V c and its error against the previous estimate, one
     // launch on the side stream (c in device memory or mapped host memory)
     auto estimate_and_error = [&](const double *c_dev) {
-      krylov_check_kernel<R><<<blocks, kRedThreads, 0, sd>>>(
-          V, n, m, c_dev, sc, yi, have_prev ? yb + (size_t)((i + 1) & 1) * n : nullptr, n,
-          rp_side, tk_side, mir_dev + 512);
+      const R *yprev = have_prev ? yb + (size_t)((i + 1) & 1) * n : nullptr;
+      if (n <= kCheckShortN)
+        krylov_check_kernel<R, 4><<<vec_blocks(4 * n), kRedThreads, 0, sd>>>(
+            V, n, m, c_dev, sc, yi, yprev, n, rp_side, tk_side, mir_dev + 512);
+      else
+        krylov_check_kernel<R, 1><<<blocks, kRedThreads, 0, sd>>>(
+            V, n, m, c_dev, sc, yi, yprev, n, rp_side, tk_side, mir_dev + 512);
       count_launch();
       if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 4], sd));
       LMG_CUDA(cudaEventRecord(ev_check_, sd));
