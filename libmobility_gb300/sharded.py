@@ -141,6 +141,27 @@ class ShardedLanczos:
                 off += cnt
         return self._full
 
+    def gather_positions(self, pos_local):
+        """All N positions (N, 3) from every rank's own particles (its rows,
+        shape (e_r - b_r, 3)): the all-gather a rank does once per
+        setPositions when it holds only its own particles."""
+        pos_local = torch.as_tensor(pos_local).reshape(-1, 3)
+        n_r = self.row_end - self.row_begin
+        if pos_local.shape[0] != n_r:
+            raise RuntimeError("[libmobility_gb300] local positions must hold this rank's rows")
+        if self.world_size == 1:
+            return pos_local.clone()
+        pad = max(e - b for b, e in self.rows)
+        send = torch.zeros((pad, 3), dtype=pos_local.dtype, device=pos_local.device)
+        send[:n_r] = pos_local
+        host = self._host_comm and send.is_cuda
+        if host:
+            send = send.cpu()
+        recv = [torch.empty_like(send) for _ in range(self.world_size)]
+        dist.all_gather(recv, send, group=self.group)
+        out = torch.cat([recv[r][: e - b] for r, (b, e) in enumerate(self.rows)])
+        return out.to(pos_local.device) if host else out
+
     # -- the solve ---------------------------------------------------------
     def _register(self, steps):  # LanczosAlgorithm.cu:224-232
         if steps - 2 > self.check_convergence_steps:

@@ -78,6 +78,40 @@ def _solve(name, oracle):
     return lz.row_begin, lz.row_end, out
 
 
+def _pos_worker(rank, ws, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(ws))
+    import torch
+    import torch.distributed as dist
+    from libmobility_gb300.sharded import ShardedLanczos
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    try:
+        N = 103
+        full = torch.arange(3 * N, dtype=torch.float64).reshape(N, 3)
+        lz = ShardedLanczos(N, dtype=torch.float64)
+        got = lz.gather_positions(full[lz.row_begin:lz.row_end])
+        q.put((rank, bool(torch.equal(got, full))))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_gather_positions_three_ranks():
+    """Each of three ranks holds only its own particles' positions; the
+    all-gather rebuilds all N in order on every rank."""
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_pos_worker, args=(r, 3, port, q)) for r in range(3)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res == [(0, True), (1, True), (2, True)]
+
+
 def _worker(rank, ws, port, name, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
                       WORLD_SIZE=str(ws))
