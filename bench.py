@@ -618,7 +618,7 @@ def ensemble_systems(rng, nsys=256):
     return sizes, geoms, np.concatenate(pos)
 
 
-def ensemble_comparison(torch, steps, warmup, rank, nsys=256, sequential=True):
+def ensemble_comparison(torch, steps, warmup, rank, nsys=256, sequential=True, peak=None):
     """Batched ensemble of 256 uneven systems (open and wall mixed) in one
     handle, FP32, tolerance 1e-6: Mdot and sqrtMdotW for all systems per call,
     against one NBody solver per system run one after the other."""
@@ -653,6 +653,9 @@ def ensemble_comparison(torch, steps, warmup, rank, nsys=256, sequential=True):
     e1.record()
     e1.synchronize()
     t_mdot = e0.elapsed_time(e1) * 1e-3 / reps
+    # credited flops of one product of all systems: open UF 36, wall UF 160 per pair
+    flops = float(sum(float(n) ** 2 * FLOPS_PER_PAIR[("wall" if gm else "open", False)]
+                      for n, gm in zip(sizes, geoms)))
     times, lat, its_all = [], [], []
     for k, dW in enumerate(dWs):
         torch.cuda.synchronize()
@@ -690,6 +693,10 @@ def ensemble_comparison(torch, steps, warmup, rank, nsys=256, sequential=True):
         "setup_and_autotune_s": setup_s,
         "mdot_ms": t_mdot * 1e3,
         "mdot_pair_interactions_per_s": pairs / t_mdot,
+        "mdot_achieved_tflops": flops / t_mdot / 1e12,
+        "mdot_frac_of_fp32_peak": flops / t_mdot / 1e12 / peak if peak else None,
+        "flops_note": "open UF 36 and wall UF 160 credited flops per pair; padding dummies "
+                      "earn nothing",
         "sqrtMdotW_ms_per_call": t_sqrt * 1e3,
         "system_solves_per_s": len(sizes) / t_sqrt,
         "sqrtMdotW_pair_interactions_per_s": sqrt_pairs / t_sqrt,
@@ -999,7 +1006,7 @@ def run_ours(args, w, ws, rank, local):
         cmp["network_gemm"] = precond_network_gemms(torch, lib)
     ens = None
     if not args.skip_ensemble:
-        ens = ensemble_comparison(torch, max(2, args.steps), 2, rank)
+        ens = ensemble_comparison(torch, max(2, args.steps), 2, rank, peak=peak)
     large = large_sqrt = None
     if not args.skip_large:
         large = large_wall_mdot(torch, rank)
