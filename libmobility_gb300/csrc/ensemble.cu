@@ -446,7 +446,7 @@ template <class R> class Ensemble final : public EnsembleBase {
     DeviceBuffer<int> sys_begin;
     MdotPlan plan;
     bool tuned = false;
-    std::vector<std::pair<int, double>> trials;  // (nsplit, ms)
+    std::vector<std::pair<int, double>> trials;  // (1000 tpt + nsplit, ms)
     // this group's share of the split scratch, so groups can run at once
     size_t part_off = 0, ticket_off = 0;
     double work = 0;  // pair flops of one product (padded sizes)
@@ -828,13 +828,19 @@ template <class R> void Ensemble<R>::ensure_plans() {
       std::vector<int> cand = {base.nsplit};
       for (int c : {1, 2, 4, 8, 16, 32, 64})
         if (c <= std::max(1, g.span / kPad)) cand.push_back(c);
+      // targets per thread (1 or 2) x source splits
       std::vector<MdotPlan> plans;
-      for (int c : cand) {
-        MdotPlan p;
-        LMG_CUDA(mdot_plan<R>(shape(g), N, g.span, sms(), 1, c, p));
-        bool dup = false;
-        for (auto &q : plans) dup = dup || q.nsplit == p.nsplit;
-        if (!dup) plans.push_back(p);
+      for (int tpt : {1, 2}) {
+        for (int c : cand) {
+          MdotPlan p;
+          if (mdot_plan<R>(shape(g), N, g.span, sms(), tpt, c, p) != cudaSuccess) {
+            (void)cudaGetLastError();
+            continue;
+          }
+          bool dup = false;
+          for (auto &q : plans) dup = dup || (q.nsplit == p.nsplit && q.tpt == p.tpt);
+          if (!dup) plans.push_back(p);
+        }
       }
       double best = 1e300;
       for (auto &p : plans) {
@@ -847,7 +853,7 @@ template <class R> void Ensemble<R>::ensure_plans() {
         LMG_CUDA(cudaEventSynchronize(ev_t1_));
         float ms = 0;
         LMG_CUDA(cudaEventElapsedTime(&ms, ev_t0_, ev_t1_));
-        g.trials.emplace_back(p.nsplit, ms / 3.0);
+        g.trials.emplace_back(p.tpt * 1000 + p.nsplit, ms / 3.0);
         if (ms < best) {
           best = ms;
           base = p;
@@ -1180,7 +1186,8 @@ template <class R> std::string Ensemble<R>::describe() const {
       << g.plan.threads * g.plan.tpt << ", \"source_splits\": " << g.plan.nsplit
       << ", \"sources_per_split\": " << g.plan.chunk << ", \"trials_ms\": [";
     for (size_t t = 0; t < g.trials.size(); t++)
-      o << (t ? ", " : "") << "[" << g.trials[t].first << ", " << g.trials[t].second << "]";
+      o << (t ? ", " : "") << "[" << g.trials[t].first / 1000 << ", "
+        << g.trials[t].first % 1000 << ", " << g.trials[t].second << "]";
     o << "]}";
   }
   o << "]}";
