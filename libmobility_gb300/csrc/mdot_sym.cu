@@ -241,40 +241,68 @@ __device__ __forceinline__ unsigned rotation_step2(const SymArgs &a, const Slot 
   return (mr0 < 4.0f ? 1u : 0u) | (mr1 < 4.0f ? 2u : 0u);
 }
 
+__device__ __forceinline__ float comp4(const float4 &v, int r) {
+  return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ void set_comp4(float4 &v, int r, float x) {
+  if (r == 0) v.x = x; else if (r == 1) v.y = x; else if (r == 2) v.z = x; else v.w = x;
+}
+__device__ __forceinline__ float sel4(const float (&v)[4], int q) {
+  return q == 0 ? v[0] : (q == 1 ? v[1] : (q == 2 ? v[2] : v[3]));
+}
+
 // For a step whose pairs were all taken in the fast form: adds (exact - fast)
-// for those closer than 2a, to the lane's sums and to slot s's j sums.
+// for those closer than 2a, to the lane's sums and to slot s's j sums.  The
+// distances of the step's 16 pairs give a mask first; only the near pairs
+// (rare) are then evaluated, in (q, r) order.
 __device__ __forceinline__ void correct_step(const SymArgs &a, const Slot &I, V3p (&ui)[4],
                                              const float4 *J4, float4 *A4, int s) {
   const float4 X = J4[s], Y = J4[32 + s], Z = J4[64 + s];
-  const float4 FX = J4[96 + s], FY = J4[128 + s], FZ = J4[160 + s];
-  const float xs[4] = {X.x, X.y, X.z, X.w}, ys[4] = {Y.x, Y.y, Y.z, Y.w};
-  const float zs[4] = {Z.x, Z.y, Z.z, Z.w}, fxs[4] = {FX.x, FX.y, FX.z, FX.w};
-  const float fys[4] = {FY.x, FY.y, FY.z, FY.w}, fzs[4] = {FZ.x, FZ.y, FZ.z, FZ.w};
-  const float4 AX = A4[s], AY = A4[32 + s], AZ = A4[64 + s];
-  float ax[4] = {AX.x, AX.y, AX.z, AX.w}, ay[4] = {AY.x, AY.y, AY.z, AY.w};
-  float az[4] = {AZ.x, AZ.y, AZ.z, AZ.w};
+  unsigned mask = 0u;
 #pragma unroll
   for (int q = 0; q < 4; q++) {
 #pragma unroll
     for (int r = 0; r < 4; r++) {
-      const float dx = I.x[q] - xs[r], dy = I.y[q] - ys[r], dz = I.z[q] - zs[r];
+      const float dx = I.x[q] - comp4(X, r), dy = I.y[q] - comp4(Y, r),
+                  dz = I.z[q] - comp4(Z, r);
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      if (r2 < 4.0f) {
-        float fe, Ge, ff, Gf;
-        exact_coeffs(a.k, r2, fe, Ge);
-        fast_coeffs(a, r2, ff, Gf);
-        const float df = fe - ff, dG = Ge - Gf;
-        float ux = 0.f, uy = 0.f, uz = 0.f;
-        apply(df, dG, dx, dy, dz, fxs[r], fys[r], fzs[r], ux, uy, uz);
-        apply(df, dG, dx, dy, dz, I.fx[q], I.fy[q], I.fz[q], ax[r], ay[r], az[r]);
-        const int h = r & 1;
-        add_lane(ui[q].x, h, ux); add_lane(ui[q].y, h, uy); add_lane(ui[q].z, h, uz);
+      if (r2 < 4.0f) mask |= 1u << (4 * q + r);
+    }
+  }
+  if (mask == 0u) return;
+  const float4 FX = J4[96 + s], FY = J4[128 + s], FZ = J4[160 + s];
+  float4 AX = A4[s], AY = A4[32 + s], AZ = A4[64 + s];
+  while (mask) {
+    const int b = __ffs(mask) - 1;
+    mask &= mask - 1u;
+    const int q = b >> 2, r = b & 3;
+    const float xj = comp4(X, r), yj = comp4(Y, r), zj = comp4(Z, r);
+    const float dx = sel4(I.x, q) - xj, dy = sel4(I.y, q) - yj, dz = sel4(I.z, q) - zj;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float fe, Ge, ff, Gf;
+    exact_coeffs(a.k, r2, fe, Ge);
+    fast_coeffs(a, r2, ff, Gf);
+    const float df = fe - ff, dG = Ge - Gf;
+    float ux = 0.f, uy = 0.f, uz = 0.f;
+    apply(df, dG, dx, dy, dz, comp4(FX, r), comp4(FY, r), comp4(FZ, r), ux, uy, uz);
+    float ax = comp4(AX, r), ay = comp4(AY, r), az = comp4(AZ, r);
+    apply(df, dG, dx, dy, dz, sel4(I.fx, q), sel4(I.fy, q), sel4(I.fz, q), ax, ay, az);
+    set_comp4(AX, r, ax);
+    set_comp4(AY, r, ay);
+    set_comp4(AZ, r, az);
+    const int h = r & 1;
+#pragma unroll
+    for (int qq = 0; qq < 4; qq++) {
+      if (qq == q) {
+        add_lane(ui[qq].x, h, ux);
+        add_lane(ui[qq].y, h, uy);
+        add_lane(ui[qq].z, h, uz);
       }
     }
   }
-  A4[s] = make_float4(ax[0], ax[1], ax[2], ax[3]);
-  A4[32 + s] = make_float4(ay[0], ay[1], ay[2], ay[3]);
-  A4[64 + s] = make_float4(az[0], az[1], az[2], az[3]);
+  A4[s] = AX;
+  A4[32 + s] = AY;
+  A4[64 + s] = AZ;
 }
 
 // Pairs inside the lane's own slot (q < r) and the self pairs, exactly.
