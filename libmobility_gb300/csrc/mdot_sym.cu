@@ -405,18 +405,16 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
         if (rotation_step(a, I, ui, J4, A4, (lane + k) & 31)) near |= 1u << (k - k0);
         __syncwarp();
       }
-      if (__any_sync(0xffffffffu, near != 0u)) {
-        // in step order: at one step the lanes' slots are all different
-        for (int kk = 0; kk < n; kk++) {
-          const bool mine = (near >> kk) & 1u;
-          if (__any_sync(0xffffffffu, mine)) {
-            if (mine) {
-              const int kabs = k0 + kk;
-              correct_step(a, I, ui, J4, A4, (lane + (diag && kabs == 0 ? 16 : kabs)) & 31);
-            }
-            __syncwarp();
-          }
+      // the flagged steps of any lane, in step order (at one step the lanes'
+      // slots are all different)
+      for (unsigned steps = __reduce_or_sync(0xffffffffu, near); steps != 0u;
+           steps &= steps - 1u) {
+        const int kk = __ffs(steps) - 1;
+        if ((near >> kk) & 1u) {
+          const int kabs = k0 + kk;
+          correct_step(a, I, ui, J4, A4, (lane + (diag && kabs == 0 ? 16 : kabs)) & 31);
         }
+        __syncwarp();
       }
       // ---- publish this warp's sums for the pair ----
       const int seg = gw - (pseg >> 8);
