@@ -281,7 +281,7 @@ __device__ __forceinline__ void correct_step(const SymArgs &a, const Slot &I, V3
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     float fe, Ge, ff, Gf;
     exact_coeffs(a.k, r2, fe, Ge);
-    fast_coeffs(a, r2, ff, Gf);
+    fast_coeffs(a, 4.0f, ff, Gf);  // the fast form clamps r^2 < 4 to 4
     const float df = fe - ff, dG = Ge - Gf;
     float ux = 0.f, uy = 0.f, uz = 0.f;
     apply(df, dG, dx, dy, dz, comp4(FX, r), comp4(FY, r), comp4(FZ, r), ux, uy, uz);
