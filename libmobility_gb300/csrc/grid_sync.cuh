@@ -54,19 +54,24 @@ __device__ __forceinline__ bool grid_barrier_mono(unsigned long long *count) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
+    // arrival with release semantics at GPU scope (cumulative: it publishes
+    // the block's writes ordered before it by the __syncthreads above), polls
+    // with acquire semantics (the __syncthreads below extends them to the
+    // block): no separate fences on either side
     const unsigned long long g = gridDim.x;
-    const unsigned long long old = atomicAdd(count, 1ull);
+    unsigned long long old;
+    asm volatile("atom.release.gpu.add.u64 %0, [%1], 1;" : "=l"(old) : "l"(count) : "memory");
     const unsigned long long target = (old / g + 1) * g;
     int ok = 0;
     for (long it = 0; it < kMonoSpins; it++) {
-      if (*(volatile unsigned long long *)count >= target) {
+      unsigned long long v;
+      asm volatile("ld.acquire.gpu.u64 %0, [%1];" : "=l"(v) : "l"(count) : "memory");
+      if (v >= target) {
         ok = 1;
         break;
       }
       if (it > 4096) __nanosleep(32);
     }
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();
