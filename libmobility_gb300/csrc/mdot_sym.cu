@@ -22,7 +22,7 @@ constexpr long long kSymMinSteps = 4;
 // line far from the origin (their own sums are never read).
 constexpr float kPadX = 1.0e6f;
 constexpr int kElems = 3 * kSymTile;  // floats of one partial slot
-constexpr int kFoldH = 3;              // output elements a thread folds per pass
+constexpr int kFoldH = 2;              // pairs of output elements a thread folds per pass
 
 struct SymArgs {
   const float *pos;
@@ -469,34 +469,37 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
     a.trace[2 * (size_t)gridDim.x * (kSymThreads / 32) + 2 * gridDim.x + blockIdx.x] = smid;
   }
-  // kFoldH elements per thread and pass, sixteen loads of each in flight (at
-  // N = 4096 one pass covers every element)
+  // kFoldH pairs of adjacent output elements per thread and pass, sixteen
+  // float2 loads of each in flight: a warp's lanes read 8 consecutive elements
+  // of each of rt slots (whole 32-byte sectors); at N = 4096 one pass covers
+  // every element
   const int rt = 1 << a.lg_rt;
-  const unsigned total = (unsigned)a.ntiles * kElems * rt;
+  constexpr int kPairs = kElems / 2;
+  const unsigned total = (unsigned)a.ntiles * kPairs * rt;
   const unsigned stride = gridDim.x * blockDim.x;
   for (unsigned base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
        base += kFoldH * stride) {
-    float S[kFoldH], C[kFoldH];
+    float S[kFoldH][2], C[kFoldH][2];
     int t[kFoldH], e[kFoldH], sub[kFoldH], cnt[kFoldH];
     bool in[kFoldH];
-    const float *src[kFoldH];
+    const float2 *src[kFoldH];
     int cmx = 0;
 #pragma unroll
     for (int h = 0; h < kFoldH; h++) {
-      S[h] = C[h] = 0.f;
+      S[h][0] = S[h][1] = C[h][0] = C[h][1] = 0.f;
       const unsigned g = base + h * stride + lane;
       in[h] = g < total;
-      const unsigned el = in[h] ? g >> a.lg_rt : 0u;
+      const unsigned el = in[h] ? g >> a.lg_rt : 0u;  // pair of elements (2 el, 2 el + 1)
       sub[h] = (int)(g & (unsigned)(rt - 1));
-      t[h] = (int)(el / kElems);
-      e[h] = (int)(el - (unsigned)t[h] * kElems);
-      src[h] = a.part + (size_t)t[h] * a.cmax * kElems + e[h];
+      t[h] = (int)(el / kPairs);
+      e[h] = 2 * (int)(el - (unsigned)t[h] * kPairs);
+      src[h] = reinterpret_cast<const float2 *>(a.part + (size_t)t[h] * a.cmax * kElems + e[h]);
       cnt[h] = in[h] ? a.cmax : 0;
       cmx = max(cmx, cnt[h]);
     }
     // each tile's slot range, in slot order (share `sub` of every rt)
     for (int m0 = 0; m0 < cmx; m0 += 16 * rt) {
-      float v[kFoldH][16];
+      float2 v[kFoldH][16];
 #pragma unroll
       for (int h = 0; h < kFoldH; h++)
 #pragma unroll
@@ -505,29 +508,38 @@ __global__ void __launch_bounds__(kSymThreads, MINB) mdot_sym_kernel(const SymAr
           v[h][m] = (j < cnt[h] &&
                      LMG_IN_BOUNDS(((size_t)t[h] * a.cmax + j + 1) * kElems <= a.part_elems, 13,
                                    t[h]))
-                        ? __ldcg(src[h] + (size_t)j * kElems) : 0.f;
+                        ? __ldcg(src[h] + (size_t)j * kPairs) : make_float2(0.f, 0.f);
         }
 #pragma unroll
       for (int h = 0; h < kFoldH; h++)
 #pragma unroll
-        for (int m = 0; m < 16; m++) fold(S[h], C[h], v[h][m]);
+        for (int m = 0; m < 16; m++) {
+          fold(S[h][0], C[h][0], v[h][m].x);
+          fold(S[h][1], C[h][1], v[h][m].y);
+        }
     }
 #pragma unroll
     for (int h = 0; h < kFoldH; h++) {
-      // combine the rt shares (the same value lands in every lane of a group)
-      for (int o = 1; o < rt; o <<= 1) {
-        const float S2 = __shfl_xor_sync(0xffffffffu, S[h], o);
-        const float C2 = __shfl_xor_sync(0xffffffffu, C[h], o);
-        const float sm = S[h] + S2;
-        const float bp = sm - S[h];
-        const float err = (S[h] - (sm - bp)) + (S2 - bp);  // exact, symmetric in (S, S2)
-        C[h] = (C[h] + C2) + err;
-        S[h] = sm;
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        // combine the rt shares (the same value lands in every lane of a group)
+        for (int o = 1; o < rt; o <<= 1) {
+          const float S2 = __shfl_xor_sync(0xffffffffu, S[h][c], o);
+          const float C2 = __shfl_xor_sync(0xffffffffu, C[h][c], o);
+          const float sm = S[h][c] + S2;
+          const float bp = sm - S[h][c];
+          const float err = (S[h][c] - (sm - bp)) + (S2 - bp);  // exact, symmetric in (S, S2)
+          C[h][c] = (C[h][c] + C2) + err;
+          S[h][c] = sm;
+        }
       }
       if (in[h] && sub[h] == 0) {
         const int2 td = tile_desc(a, t[h]);
-        if (e[h] < 3 * td.y && LMG_IN_BOUNDS(3 * (size_t)td.x + e[h] < 3 * (size_t)a.N, 14, td.x))
-          a.U[3 * (size_t)td.x + e[h]] = S[h] + C[h];
+#pragma unroll
+        for (int c = 0; c < 2; c++)
+          if (e[h] + c < 3 * td.y &&
+              LMG_IN_BOUNDS(3 * (size_t)td.x + e[h] + c < 3 * (size_t)a.N, 14, td.x))
+            a.U[3 * (size_t)td.x + e[h] + c] = S[h][c] + C[h][c];
       }
     }
   }
