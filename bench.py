@@ -1001,8 +1001,8 @@ def run_ours(args, w, ws, rank, local):
     cmp = None
     if not args.skip_precond:
         # the preconditioned stopping step moves by +-4 from one dW to the next:
-        # at least 8 solves per arm
-        cmp = sqrtmdotw_comparison(torch, max(8, args.steps), 2, rank)
+        # at least 12 solves per arm
+        cmp = sqrtmdotw_comparison(torch, max(12, args.steps), 2, rank)
         cmp["network_gemm"] = precond_network_gemms(torch, lib)
     ens = None
     if not args.skip_ensemble:
