@@ -91,7 +91,8 @@ template <class R> class Solver final : public SolverBase {
     release_all();
     for (auto &e : ev_iter_)
       if (e) cudaEventDestroy(e);
-    if (ev_check_) cudaEventDestroy(ev_check_);
+    for (auto &e : ev_check_)
+      if (e) cudaEventDestroy(e);
     if (ev_side_) cudaEventDestroy(ev_side_);
     for (auto &e : ev_phase_)
       if (e) cudaEventDestroy(e);
@@ -138,7 +139,8 @@ template <class R> class Solver final : public SolverBase {
   // iteration j completes ev_iter_[j % kIterEvents] (a ring: up to kMaxLookahead
   // iterations run ahead of the check being evaluated)
   static constexpr int kMaxLookahead = 4, kIterEvents = kMaxLookahead + 2;
-  cudaEvent_t ev_iter_[kIterEvents] = {}, ev_check_ = nullptr, ev_side_ = nullptr;
+  // ev_check_[i & 1]: the check of iteration i done (two checks in flight)
+  cudaEvent_t ev_iter_[kIterEvents] = {}, ev_check_[2] = {}, ev_side_ = nullptr;
   // phase timing: per iteration j, [5j, 5j+1] bracket the operator, [5j+1,
   // 5j+2] the vector updates and [5j+3, 5j+4] the check; ev_pre_ the
   // preconditioner build and P solve (created on the first timed solve)
@@ -572,7 +574,7 @@ template <class R> void Solver<R>::ensure_side() {
     LMG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     LMG_CUDA(cudaStreamCreateWithPriority(&side_, cudaStreamNonBlocking, hi));
     for (auto &e : ev_iter_) LMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    LMG_CUDA(cudaEventCreateWithFlags(&ev_check_, cudaEventDisableTiming));
+    for (auto &e : ev_check_) LMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     LMG_CUDA(cudaEventCreateWithFlags(&ev_side_, cudaEventDisableTiming));
   }
 }
@@ -778,6 +780,31 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
   // host, so with cheap matrix-vector products several iterations keep the
   // GPU busy meanwhile; past convergence they are discarded
   int ahead = nper_lookahead();
+  // A check is read one check late: the check of iteration i is launched,
+  // then the error of the previous check (whose kernel has finished by then)
+  // decides, so the host never waits on a check it just launched while the
+  // GPU drains its queue.  The stopping step and result are the same as
+  // deciding at once (the later launches are discarded); the error slots,
+  // estimate buffers and host c slots alternate by iteration parity, and a
+  // slot is reused only after the check that used it was read.
+  int pend_i = -1;
+  bool pend_tested = false;
+  auto resolve = [&](int pi, bool tested) {
+    LMG_CUDA(cudaEventSynchronize(ev_check_[pi & 1]));
+    if (mir[516] != 0.0)
+      throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
+    err = tested ? mir[512 + (pi & 1)] : HUGE_VAL;
+    if (tested) {  // the reference never tests the first estimate (i > 0 there)
+      if (residual) *residual = err;
+      if (std::isnan(err))
+        throw Error(LMG_ERR_NAN, "[Lanczos] Unknown error (found NaN in result guess)");
+    }
+    if (cb_ && pi > 0) cb_(pi, err, cb_user_);
+    if (tested && err <= tol) {
+      lanczos_register(pi);
+      done = pi;
+    }
+  };
   for (int i = 0; i < limit; i++) {
     while (issued <= i + ahead && issued < limit) issue(issued);
     if (!(i >= k || cb_ != nullptr)) continue;
@@ -788,17 +815,17 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     // launch on the side stream (c in device memory or mapped host memory)
     auto estimate_and_error = [&](const double *c_dev) {
       const R *yprev = have_prev ? yb + (size_t)((i + 1) & 1) * n : nullptr;
+      double *e_out = mir_dev + 512 + (i & 1);
       if (n <= kCheckShortN)
         krylov_check_kernel<R, 4><<<vec_blocks(4 * n), kRedThreads, 0, sd>>>(
-            V, n, m, c_dev, sc, yi, yprev, n, rp_side, tk_side, mir_dev + 512);
+            V, n, m, c_dev, sc, yi, yprev, n, rp_side, tk_side, e_out);
       else
         krylov_check_kernel<R, 1><<<blocks, kRedThreads, 0, sd>>>(
-            V, n, m, c_dev, sc, yi, yprev, n, rp_side, tk_side, mir_dev + 512);
+            V, n, m, c_dev, sc, yi, yprev, n, rp_side, tk_side, e_out);
       count_launch();
       if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 4], sd));
-      LMG_CUDA(cudaEventRecord(ev_check_, sd));
+      LMG_CUDA(cudaEventRecord(ev_check_[i & 1], sd));
       LMG_CUDA(cudaGetLastError());
-      LMG_CUDA(cudaEventSynchronize(ev_check_));
     };
     NvtxRange nvtx_check("lmg Lanczos check");
     const int sqrt_mode = g_lanczos_device_sqrt.load();
@@ -810,12 +837,13 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
       tridiag_sqrt_quad_kernel<<<1, kQuadThreads, 0, sd>>>(sc, m, cd, quad_g, mir_dev + 520);
       count_launch();
       estimate_and_error(cd);
+      LMG_CUDA(cudaEventSynchronize(ev_check_[i & 1]));  // for the fallback flag
       if (mir[516] != 0.0)
         throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
       on_host = mir[520] != 0.0;  // not positive definite or too ill-conditioned
     }
     if (on_host) {
-      // the exact eigen-solution of T on the host (implicit QL, FP64)
+      // T^{1/2} e1 on the host (quadrature, or the exact implicit QL; FP64)
       LMG_CUDA(cudaEventSynchronize(ev_iter_[i % kIterEvents]));
       if (mir[516] != 0.0)
         throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
@@ -832,28 +860,22 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
                              ql_work_.data() + 512, log, c);
       if (rc != 0)
         for (int q = 0; q < m; q++) c[q] = std::nan("");
-      // c is read by the kernel from mapped host memory: this slot is not
-      // written again before the check two later, after this one completed
+      // c is read by the kernel from mapped host memory: this slot is written
+      // again two checks later, after this check was read
       LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i % kIterEvents], 0));
       if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
       estimate_and_error(hc_.device_ptr() + (i & 1) * kMaxLanczosIterations);
     }
     if (timing_) checked.push_back(i);
-    err = have_prev ? mir[512] : HUGE_VAL;
-    if (have_prev) {  // the reference never tests the first estimate (i > 0 there)
-      if (residual) *residual = err;
-      if (std::isnan(err))
-        throw Error(LMG_ERR_NAN, "[Lanczos] Unknown error (found NaN in result guess)");
+    if (pend_i >= 0) {
+      resolve(pend_i, pend_tested);
+      if (done >= 0) break;
     }
-    if (cb_ && i > 0) cb_(i, err, cb_user_);
-    const bool tested = have_prev;
+    pend_i = i;
+    pend_tested = have_prev;
     have_prev = true;
-    if (tested && err <= tol) {
-      lanczos_register(i);
-      done = i;
-      break;
-    }
   }
+  if (done < 0 && pend_i >= 0) resolve(pend_i, pend_tested);
   if (done < 0) {
     LMG_CUDA(cudaStreamSynchronize(st));
     throw Error(LMG_ERR_NO_CONVERGENCE, "[Lanczos] Could not converge");

@@ -175,8 +175,10 @@ def test_adaptive_check_schedule_matches_reference(cuda, oracle):
 def test_phase_timing_counts_and_leaves_results_unchanged(cuda):
     """The measurement hook only records events: two solvers with the same
     history, one timed, give bitwise the same results; the sums count every
-    issued iteration (up to 3 issued ahead of the last check at this size
-    included) and the algorithmic bytes 4 n s per iteration."""
+    issued iteration (up to 3 issued ahead of the check being evaluated at
+    this size, and the checks are read one check late: up to 5 past the
+    stopping step per solve) and the algorithmic bytes 4 n s per
+    iteration."""
     rng = np.random.default_rng(12)
     N = 300
     p = np.column_stack([rng.uniform(0, 40, (N, 2)), rng.uniform(1.5, 10, N)])
@@ -196,7 +198,7 @@ def test_phase_timing_counts_and_leaves_results_unchanged(cuda):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
         its += b[2]
     assert t["solves"] == 4 and t["checks"] >= 4
-    assert its <= t["iterations"] <= its + 4 * 4
+    assert its <= t["iterations"] <= its + 4 * 5
     assert t["vector_bytes"] == 4 * (6 * N) * 4 * t["iterations"]
     assert t["check_bytes"] > 0 and t["vector_ms"] > 0 and t["check_ms"] > 0
     assert t["operator_ms"] > 0 and t["build_ms"] == 0 and t["psolve_ms"] == 0
