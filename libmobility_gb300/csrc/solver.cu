@@ -789,15 +789,21 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
   // slot is reused only after the check that used it was read.
   int pend_i = -1;
   bool pend_tested = false;
+  // a solve that ends in an error may leave the next check running on the
+  // side stream; the next solve resets the tickets that check uses from the
+  // main stream, so the side stream is drained before the error is raised
+  auto fail = [&](lmg_status code, const char *msg) {
+    cudaStreamSynchronize(sd);
+    throw Error(code, msg);
+  };
   auto resolve = [&](int pi, bool tested) {
     LMG_CUDA(cudaEventSynchronize(ev_check_[pi & 1]));
     if (mir[516] != 0.0)
-      throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
+      fail(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
     err = tested ? mir[512 + (pi & 1)] : HUGE_VAL;
     if (tested) {  // the reference never tests the first estimate (i > 0 there)
       if (residual) *residual = err;
-      if (std::isnan(err))
-        throw Error(LMG_ERR_NAN, "[Lanczos] Unknown error (found NaN in result guess)");
+      if (std::isnan(err)) fail(LMG_ERR_NAN, "[Lanczos] Unknown error (found NaN in result guess)");
     }
     if (cb_ && pi > 0) cb_(pi, err, cb_user_);
     if (tested && err <= tol) {
@@ -839,14 +845,14 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
       estimate_and_error(cd);
       LMG_CUDA(cudaEventSynchronize(ev_check_[i & 1]));  // for the fallback flag
       if (mir[516] != 0.0)
-        throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
+        fail(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
       on_host = mir[520] != 0.0;  // not positive definite or too ill-conditioned
     }
     if (on_host) {
       // T^{1/2} e1 on the host (quadrature, or the exact implicit QL; FP64)
       LMG_CUDA(cudaEventSynchronize(ev_iter_[i % kIterEvents]));
       if (mir[516] != 0.0)
-        throw Error(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
+        fail(LMG_ERR_TIMEOUT, "[libmobility_gb300] Lanczos step: grid barrier timed out");
       for (int q = 0; q < m; q++) {
         al[q] = mir[2 * q];
         be[q] = mir[2 * q + 1];
