@@ -134,6 +134,7 @@ def load():
         "lmg_internal_classify_pointer": [_I, _I, _I],
         "lmg_internal_lanczos_device_sqrt": [_I],
         "lmg_internal_lanczos_lookahead": [_I],
+        "lmg_internal_lanczos_check_wait": [_I],
     }
     for name, args in internal.items():
         fn = getattr(lib, name)

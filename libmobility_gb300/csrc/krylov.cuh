@@ -906,8 +906,20 @@ __global__ void krylov_check_kernel(const R *V, size_t ldv, int m, const double 
     const size_t e = e0 + tid / TPE;
     const bool ok = e < n;
     R acc = 0;
-    if (ok)
-      for (int k = part; k < m; k += TPE) acc += cs[k] * V[(size_t)k * ldv + e];
+    if (ok) {
+      // eight loads in flight per thread ahead of their products, which are
+      // summed in the same order as one at a time
+      const R *col = V + e;
+      int k = part;
+      for (; k + 7 * TPE < m; k += 8 * TPE) {
+        R x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) x[u] = col[(size_t)(k + u * TPE) * ldv];
+#pragma unroll
+        for (int u = 0; u < 8; u++) acc += cs[k + u * TPE] * x[u];
+      }
+      for (; k < m; k += TPE) acc += cs[k] * col[(size_t)k * ldv];
+    }
 #pragma unroll
     for (int o = 1; o < TPE; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (ok && part == 0) {

@@ -19,6 +19,10 @@ extern std::atomic<int> g_sym_mode, g_sym_warps, g_sym_variant;
 extern std::atomic<int> g_lanczos_device_sqrt;
 // iterations issued ahead of a check (0 = by batch size: 3 up to 8192 particles, else 1)
 extern std::atomic<int> g_lanczos_lookahead;
+// what the check kernel of iteration i waits for on the side stream: 0 the
+// end of iteration i; 1 the end of iteration i + 1's matrix-vector product
+// where that was issued (it then runs beside iteration i + 1's vector step)
+extern std::atomic<int> g_lanczos_check_wait;
 // the single-system Lanczos vector step: 0 (default) one thread-block
 // cluster, 1 the cooperative grid-wide launch
 extern std::atomic<int> g_lanczos_step_mode;

@@ -25,6 +25,7 @@ std::atomic<int> g_sym_mode{0}, g_sym_warps{0}, g_sym_variant{0};
 std::atomic<unsigned long long *> g_sym_trace{nullptr};
 std::atomic<int> g_lanczos_device_sqrt{2};
 std::atomic<int> g_lanczos_lookahead{0};
+std::atomic<int> g_lanczos_check_wait{0};
 std::atomic<int> g_precond_tc{0};
 std::atomic<int> g_lanczos_step_mode{0};
 std::atomic<int> g_lanczos_step_shape{0};
@@ -186,6 +187,16 @@ int lmg_internal_lanczos_device_sqrt(int on) {
 int lmg_internal_lanczos_lookahead(int n) {
   if (n < 0 || n > 4) return 1;
   lmg::g_lanczos_lookahead.store(n);
+  return 0;
+}
+
+// What each check kernel of the single-system Lanczos waits for: 0 the end
+// of its iteration, 1 the end of the next iteration's matrix-vector product
+// (it then shares the GPU with the next vector step instead of the next
+// product).  Results are the same either way.
+int lmg_internal_lanczos_check_wait(int mode) {
+  if (mode != 0 && mode != 1) return 1;
+  lmg::g_lanczos_check_wait.store(mode);
   return 0;
 }
 

@@ -91,6 +91,8 @@ template <class R> class Solver final : public SolverBase {
     release_all();
     for (auto &e : ev_iter_)
       if (e) cudaEventDestroy(e);
+    for (auto &e : ev_prod_)
+      if (e) cudaEventDestroy(e);
     for (auto &e : ev_check_)
       if (e) cudaEventDestroy(e);
     if (ev_side_) cudaEventDestroy(ev_side_);
@@ -139,8 +141,10 @@ template <class R> class Solver final : public SolverBase {
   // iteration j completes ev_iter_[j % kIterEvents] (a ring: up to kMaxLookahead
   // iterations run ahead of the check being evaluated)
   static constexpr int kMaxLookahead = 4, kIterEvents = kMaxLookahead + 2;
+  // ev_prod_ likewise the end of iteration j's matrix-vector product;
   // ev_check_[i & 1]: the check of iteration i done (two checks in flight)
-  cudaEvent_t ev_iter_[kIterEvents] = {}, ev_check_[2] = {}, ev_side_ = nullptr;
+  cudaEvent_t ev_iter_[kIterEvents] = {}, ev_prod_[kIterEvents] = {}, ev_check_[2] = {},
+              ev_side_ = nullptr;
   // phase timing: per iteration j, [5j, 5j+1] bracket the operator, [5j+1,
   // 5j+2] the vector updates and [5j+3, 5j+4] the check; ev_pre_ the
   // preconditioner build and P solve (created on the first timed solve)
@@ -574,6 +578,7 @@ template <class R> void Solver<R>::ensure_side() {
     LMG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     LMG_CUDA(cudaStreamCreateWithPriority(&side_, cudaStreamNonBlocking, hi));
     for (auto &e : ev_iter_) LMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto &e : ev_prod_) LMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (auto &e : ev_check_) LMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     LMG_CUDA(cudaEventCreateWithFlags(&ev_side_, cudaEventDisableTiming));
   }
@@ -749,6 +754,7 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
     R *vj = V + (size_t)j * n;
     if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * j], st));
     apply_operator(vj, w);
+    LMG_CUDA(cudaEventRecord(ev_prod_[j % kIterEvents], st));
     if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * j + 1], st));
     const R *vprev = j > 0 ? vj - n : vj;
     R *vnext = vj + n;
@@ -867,8 +873,13 @@ int Solver<R>::lanczos(const R *z, R *y_out, size_t n, double tol, double *resid
       if (rc != 0)
         for (int q = 0; q < m; q++) c[q] = std::nan("");
       // c is read by the kernel from mapped host memory: this slot is written
-      // again two checks later, after this check was read
-      LMG_CUDA(cudaStreamWaitEvent(sd, ev_iter_[i % kIterEvents], 0));
+      // again two checks later, after this check was read.  The kernel reads
+      // rows 0..i of V and the previous estimate, which the next product
+      // and vector step leave alone, so it may also start after the next
+      // product (check_wait 1)
+      const bool after_next = g_lanczos_check_wait.load() == 1 && issued > i + 1;
+      LMG_CUDA(cudaStreamWaitEvent(
+          sd, after_next ? ev_prod_[(i + 1) % kIterEvents] : ev_iter_[i % kIterEvents], 0));
       if (timing_) LMG_CUDA(cudaEventRecord(ev_phase_[5 * i + 3], sd));
       estimate_and_error(hc_.device_ptr() + (i & 1) * kMaxLanczosIterations);
     }

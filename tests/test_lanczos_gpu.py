@@ -285,9 +285,11 @@ def test_device_and_host_square_roots_agree(cuda, precision, wall):
 
 @pytest.mark.parametrize("precision", ["float", "double"])
 def test_lookahead_changes_nothing(cuda, precision):
-    """Issuing 1 or 3 iterations ahead of the check being evaluated only
-    changes how busy the GPU is: same stopping step, bitwise the same result
-    (the checks read nothing a later iteration writes)."""
+    """Issuing 1 or 3 iterations ahead of the check being evaluated, and
+    starting each check kernel after its own iteration or after the next
+    iteration's product, only change how busy the GPU is: same stopping
+    step, bitwise the same result (the checks read nothing a later iteration
+    writes)."""
     from libmobility_gb300 import _capi
     lib = _capi.load()
     rng = np.random.default_rng(33)
@@ -296,16 +298,20 @@ def test_lookahead_changes_nothing(cuda, precision):
     zs = [rng.normal(size=3 * N) for _ in range(3)]
     out = {}
     try:
-        for ahead in (1, 3):
+        for ahead, wait in ((1, 0), (3, 0), (1, 1), (3, 1)):
             assert lib.lmg_internal_lanczos_lookahead(ahead) == 0
+            assert lib.lmg_internal_lanczos_check_wait(wait) == 0
             s = make_solver(0, 0, 1.0, 1 / (6 * np.pi), precision)
             s.setPositions(p)
-            out[ahead] = [s.sqrtMdotW_noise(z) for z in zs]
+            out[ahead, wait] = [s.sqrtMdotW_noise(z) for z in zs]
     finally:
         lib.lmg_internal_lanczos_lookahead(0)
-    for (u1, _, it1, r1), (u3, _, it3, r3) in zip(out[1], out[3]):
-        assert it1 == it3 and r1 == r3
-        assert np.array_equal(np.asarray(u1), np.asarray(u3))
+        lib.lmg_internal_lanczos_check_wait(0)
+    assert lib.lmg_internal_lanczos_check_wait(2) != 0
+    for key in ((3, 0), (1, 1), (3, 1)):
+        for (u1, _, it1, r1), (u3, _, it3, r3) in zip(out[1, 0], out[key]):
+            assert it1 == it3 and r1 == r3
+            assert np.array_equal(np.asarray(u1), np.asarray(u3))
 
 
 @pytest.mark.parametrize("precision,wall,ang,N", [
