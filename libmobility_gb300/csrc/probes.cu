@@ -171,8 +171,8 @@ int lmg_internal_sym_plan(int N, int nper, long long resident, int force_warps, 
 // exact QL on the host; 1 on the device by quadrature; 2 (the default) on
 // the host by quadrature; the host QL wherever a quadrature does not apply.
 // Applies to the next solves of every handle.  (Measured at N = 4096, FP32,
-// tolerance 1e-6: 6.1 ms per solve with the host QL, 3.6 ms with the host
-// quadrature (18 against 296 us a check at m = 80 on a Grace core), 8.4 ms
+// tolerance 1e-6: 4.7 ms per solve with the host QL, 2.6 ms with the host
+// quadrature (18 against 296 us a check at m = 80 on a Grace core), 7.9 ms
 // on the device: there the quadrature is a chain of FP64 divisions on
 // GB300's narrow FP64 units.)
 int lmg_internal_lanczos_device_sqrt(int on) {
