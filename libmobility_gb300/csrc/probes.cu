@@ -229,10 +229,6 @@ int lmg_internal_bounds_probe(void) {
   return (int)e;
 }
 
-// Timeline of the next symmetric-kernel launches (measurement hook, off when
-// null): `buf` is device memory of 2 * (warps + blocks) 64-bit words, filled
-// with %globaltimer nanoseconds: per warp its start and the end of its
-// rotation steps, then per block the end of the grid barrier and of the fold.
 // Lanczos vector step of the single-system solver: 0 one cluster (default),
 // 1 the cooperative grid-wide launch.
 int lmg_internal_lanczos_step_mode(int mode) {

@@ -276,3 +276,30 @@ def test_buffers_of_another_gpu_are_refused():
     assert f(2, 0, 0) == 1 and f(2, 3, 3) == 1       # this GPU's memory
     assert f(2, 1, 0) == -1 and f(2, 0, 5) == -1     # another GPU's memory
     assert f(3, 1, 0) == 1                           # managed memory
+
+
+def test_solver_selectors_check_their_arguments(lib):
+    """The process-wide selectors of the single-system Lanczos and the
+    preconditioner build take only their documented values (each one sets a
+    setting, no device work) and are left at their defaults."""
+    cases = [
+        (lib.lmg_internal_lanczos_step_mode, (0, 1), (-1, 2), 0),
+        (lib.lmg_internal_lanczos_device_sqrt, (0, 1, 2), (-1, 3), 2),
+        (lib.lmg_internal_lanczos_lookahead, (0, 1, 4), (-1, 5), 0),
+        (lib.lmg_internal_lanczos_check_wait, (0, 1), (-1, 2), 0),
+        (lib.lmg_internal_precond_tc, (0, 1), (-1, 2), 0),
+    ]
+    try:
+        for fn, good, bad, _ in cases:
+            for v in good:
+                assert fn(v) == 0, (fn.__name__, v)
+            for v in bad:
+                assert fn(v) != 0, (fn.__name__, v)
+        shape = lib.lmg_internal_lanczos_step_shape
+        assert shape(16, 256) == 0 and shape(1, 32) == 0 and shape(0, 0) == 0
+        for ctas, threads in ((17, 256), (0, 256), (4, 16), (4, 100), (4, 2048)):
+            assert shape(ctas, threads) != 0, (ctas, threads)
+    finally:
+        for fn, _, _, default in cases:
+            fn(default)
+        lib.lmg_internal_lanczos_step_shape(0, 0)
