@@ -265,7 +265,7 @@ def flushed_time(torch, fn, flush, reps=20):
     return statistics.median(ts)
 
 
-def config1_inputs(seed=1234):
+def open4k_inputs(seed=1234):
     """N = 4096 uniform in the cube of volume fraction 0.05 (a = 1), forces
     N(0, 1)."""
     rng = np.random.default_rng(seed)
@@ -275,13 +275,13 @@ def config1_inputs(seed=1234):
 
 
 def open4k_mdot(torch, lib, peak32, peak64, flush):
-    """Configuration 1: open-boundary translational Mdot, N = 4096, a = 1,
+    """Open-boundary translational Mdot, N = 4096, a = 1,
     viscosity 1/(6 pi), in FP32 and FP64 on device-resident inputs.  The FP32
     handle takes the symmetric kernel; the tiled kernel's time on the same
     handle is given beside it.  Returns the sub-object and the results (for
     the error against the FP64 oracle, filled in by the caller)."""
     from libmobility_gb300 import NBody
-    pos, F = config1_inputs()
+    pos, F = open4k_inputs()
     N = pos.shape[0]
     pairs = float(N) * N
     out = {"workload": "open RPY (UF), N=4096, cube at phi=0.05, a=1, viscosity 1/(6 pi), "
@@ -323,13 +323,13 @@ def open4k_mdot(torch, lib, peak32, peak64, flush):
 
 
 def open4k_sqrt(torch, lib, solves=20):
-    """Configuration 1's square root: open boundary, N = 4096, FP32,
+    """Square root of the open N = 4096 system: open boundary, FP32,
     tolerance 1e-6, sqrtMdotW solves per second (host wall clock around each
     call, device-resident dW) with T^{1/2} e1 of the convergence checks by
     quadrature on the host (the default), by the exact QL on the host and by
     quadrature on the device, on fresh handles after 3 warm-up solves each."""
     from libmobility_gb300 import NBody
-    pos, _ = config1_inputs()
+    pos, _ = open4k_inputs()
     N = pos.shape[0]
     dpos = torch.tensor(pos, dtype=torch.float32, device="cuda")
     g = torch.Generator(device="cuda").manual_seed(17)
@@ -367,8 +367,8 @@ def reference_gpu_mdot(torch, wall16k_inputs):
     """libMobility's own NBody CUDA kernel (computeRPYBatchedFastGPU, launch
     shape of its launcher, NbodyRPY.cu:99-116), compiled for sm_103a from the
     reference sources into oracle/_ref, next to this library's Mdot on the
-    same GPU and inputs: configuration 1 (open UF, N = 4096) and configuration
-    2 (single wall, all blocks, N = 16384), FP32 and FP64, both timed as CUDA
+    same GPU and inputs: open UF, N = 4096, and single wall, all blocks,
+    N = 16384, FP32 and FP64, both timed as CUDA
     graph replays of 20 launches on device buffers."""
     import ctypes
     from oracle import build as ob
@@ -387,7 +387,7 @@ def reference_gpu_mdot(torch, wall16k_inputs):
     a, eta = 1.0, 1 / (6 * math.pi)
     t0, r0, rt0 = 1 / (6 * math.pi * eta * a), 1 / (8 * math.pi * eta * a ** 3), \
         1 / (8 * math.pi * eta * a * a)
-    pos1, F1 = config1_inputs()
+    pos1, F1 = open4k_inputs()
     pos2, F2, T2, _ = wall16k_inputs
     out = {"kernel": "computeRPYBatchedFastGPU (libMobility NbodyRPY.cu:26-97), sm_103a cubin"}
     for name, wall, ang, pos, F, T, fpp in (
@@ -711,7 +711,7 @@ def ensemble_comparison(torch, steps, warmup, rank, nsys=256, sequential=True, p
 
 
 def large_wall_mdot(torch, rank, reps=3):
-    """Configuration 5's matrix-vector product: single wall, N = 262144,
+    """Matrix-vector product of the large wall system: single wall, N = 262144,
     x, y ~ U[0, 1024), z ~ U[1.5, 40], forces and torques, includeAngular,
     FP32; CUDA events around `reps` launches on device-resident inputs (its
     FP64 check on 4096 rows is tests/test_large_gpu.py)."""
@@ -745,7 +745,7 @@ def large_wall_mdot(torch, rank, reps=3):
 
 
 def large_wall_sqrt(torch, rank):
-    """Configuration 5's square root: single wall, N = 262144, x, y ~ U[0,
+    """Square root of the large wall system: single wall, N = 262144, x, y ~ U[0,
     1024), z ~ U[1.5, 40], includeAngular, FP32, tolerance 1e-6: one
     sqrtMdotW of plain Lanczos and one with the learned wall preconditioner
     (rebuilt for the solve), same dW, wall time and iterations."""
@@ -857,7 +857,7 @@ def cpu_baseline(w, pos, F, T, seconds=8.0):
 
 
 def oracle_error_open4k(pos, F, results):
-    """Max |U - U_oracle| / max |U_oracle| of the configuration-1 products
+    """Max |U - U_oracle| / max |U_oracle| of the open N = 4096 products
     against the FP64 C oracle (all host threads), every row."""
     from oracle import build as ob
     ob.build_oracle()
@@ -1102,13 +1102,13 @@ def main():
         if rank == 0:
             print(json.dumps({"precond_network_gemm": out}))
         return
-    if args.only == "large":  # configuration 5's square roots alone
+    if args.only == "large":  # the N = 262144 wall square roots alone
         import torch
         out = large_wall_sqrt(torch, rank)
         if rank == 0:
             print(json.dumps({"wall_262k_sqrt": out}))
         return
-    if args.only == "open4k":  # configuration 1 alone (profiling runs)
+    if args.only == "open4k":  # the open N = 4096 figures alone (profiling runs)
         import torch
         from libmobility_gb300 import _capi
         lib = _capi.load()

@@ -1,6 +1,6 @@
 """FP64 CPU oracle for libMobility's NBody RPY product and Lanczos sqrt(M) dW.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker for libmobility_gb300's
+TEST INFRASTRUCTURE ONLY.  This module is the reference oracle for libmobility_gb300's
 CUDA path.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU
 baseline leg (and its ``--impl reference`` arm) import it; the product never
 does.

@@ -1,7 +1,7 @@
 /*
  * FP64 CPU oracle for the NBody Rotne-Prager-Yamakawa mobility product.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA path of
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle for the CUDA path of
  * libmobility_gb300: only tests/, __graft_entry__.smoke() and the CPU-baseline
  * leg of bench.py load it.  The product never links or calls it.
  *

@@ -316,7 +316,7 @@ def test_lookahead_changes_nothing(cuda, precision):
 
 @pytest.mark.parametrize("precision,wall,ang,N", [
     ("float", 0, 0, 300),      # one element a thread or none (registers)
-    ("float", 0, 0, 4096),     # configuration 1's size
+    ("float", 0, 0, 4096),     # the open N = 4096 workload
     ("float", 1, 1, 8000),     # 48000 elements: four a thread
     ("float", 0, 0, 40000),    # eight a thread
     ("float", 0, 0, 60000),    # streamed through memory

@@ -100,7 +100,7 @@ def test_sym_agrees_with_tiled_kernel_and_repeats_bitwise(lib):
     assert not np.array_equal(U1, Uk)  # the two kernels really are different code
 
 
-def test_sym_config1_full_rows_vs_oracle(lib, oracle):
+def test_sym_open4k_full_rows_vs_oracle(lib, oracle):
     """N = 4096 open, volume fraction 0.05, a = 1, viscosity 1/(6 pi): every row
     against the FP64 oracle."""
     rng = np.random.default_rng(2024)
