@@ -664,14 +664,18 @@ cudaError_t launch_step_cluster(int ctas, int cta_threads, R *w, const R *vi, co
 //
 // Schedule per iteration i on the solver stream S: matvec, alpha, beta (which
 // also writes alpha_i, beta_i to mapped host memory), next -> event I_i.  The
-// GPU is kept one iteration ahead: iteration i+1 is issued before the host
-// handles the convergence check of iteration i.  A check (every i >= k, the
-// adaptive start of LanczosAlgorithm.cu:179-184, or every i with a callback)
-// waits for I_i, solves the FP64 tridiagonal problem on the host while the
-// GPU runs iteration i+1, then on the high-priority side stream P computes
-// y_i = |z| V c_i and |y_i - y_{i-1}| / |y_{i-1}|, and reads the error back.
-// At the first check of a solve there is no y_{i-1}; its error counts as
-// infinite (the reference compares against a zero or stale buffer there).
+// GPU is kept ahead of the host: iterations up to i+3 (batches of up to 8192
+// particles, else i+1) are issued before the host handles the convergence
+// check of iteration i.  A check (every i >= k, the adaptive start of
+// LanczosAlgorithm.cu:179-184, or every i with a callback) waits for I_i,
+// takes the FP64 T^{1/2} e1 on the host while the GPU runs ahead, then on
+// the high-priority side stream P computes y_i = |z| V c_i and
+// |y_i - y_{i-1}| / |y_{i-1}| into mapped host memory.  That error is read
+// one check late (after check i+1 is launched), so the host never waits on
+// the check it has just launched; iterations issued past the stopping step
+// are discarded.  At the first check of a solve there is no y_{i-1}; its
+// error counts as infinite (the reference compares against a zero or stale
+// buffer there).
 template <class R> void Solver<R>::ensure_phase_events() {
   if (ev_phase_.empty()) {
     ev_phase_.assign(5 * (kMaxLanczosIterations + 1), nullptr);
