@@ -99,6 +99,35 @@ def test_errors(cuda, periodicity):
             s.Mdot(torques=np.random.rand(3 * nw))
 
 
+@pytest.mark.parametrize("nbatch,nper", [(1, 12), (12, 1)])
+def test_good_batch_parameters(cuda, nbatch, nper):
+    """test_initialization.py: NBatch x NperBatch particles are accepted."""
+    from libmobility_gb300 import NBody
+    s = NBody("open", "open", "open")
+    s.setParameters("advise", nbatch, nper)
+    s.initialize(viscosity=1.0, hydrodynamicRadius=1.5)
+    s.setPositions(np.random.rand(nbatch * nper, 3))
+
+
+def test_default_and_no_parameters(cuda):
+    """test_initialization.py: setParameters("advise") alone, and no
+    setParameters at all (default algorithm, every particle in one batch),
+    both take positions and give the same Mdot."""
+    from libmobility_gb300 import NBody
+    pos = np.random.rand(10, 3)
+    out = []
+    for with_params in (True, False):
+        s = NBody("open", "open", "open")
+        if with_params:
+            s.setParameters("advise")
+        s.initialize(viscosity=1.0, hydrodynamicRadius=1.5)
+        s.setPositions(pos)
+        mf, mt = s.Mdot(pos)
+        assert mf.shape == (10, 3) and mt is None
+        out.append(mf)
+    assert np.array_equal(out[0], out[1])
+
+
 @pytest.mark.parametrize("periodicity", CONFIGS)
 @pytest.mark.parametrize("ang", [True, False])
 def test_langevin_kbt0_equals_mdot(cuda, periodicity, ang):
