@@ -869,6 +869,15 @@ def oracle_error_open4k(pos, F, results):
     return {p: float(np.abs(u.reshape(-1) - Uo).max() / scale) for p, u in results.items()}
 
 
+def line_config(w, ws):
+    """The config object both arms print: the workload, its size and
+    tolerance, how caches are kept out of the timing, and the rank layout."""
+    return {"workload": w["desc"], "N": w["N"], "tolerance": w["tol"],
+            "l2": "GPU arm: L2 flushed between timed steps (inputs smaller than L2); "
+                  "CPU arm: no GPU, host caches as they are",
+            "parallelism": f"replicas x{ws}"}
+
+
 def run_reference(args, w, ws, rank):
     if rank != 0:
         return
@@ -883,7 +892,7 @@ def run_reference(args, w, ws, rank):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pair-interactions/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": {"workload": w["desc"]},
+            "data": "synthetic (seeded)", "config": line_config(w, ws),
             "cpu_baseline": base,
             "e2e": {"value": v, "unit": "pair-interactions/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -1026,9 +1035,7 @@ def run_ours(args, w, ws, rank, local):
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": t_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": w["desc"], "N": N, "tolerance": w["tol"],
-                   "l2": "flushed between timed steps (inputs smaller than L2)",
-                   "parallelism": f"replicas x{ws}"},
+        "config": line_config(w, ws),
         "sqrtMdotW": {"solves_per_s": 1.0 / t_sqrt, "lanczos_iterations": it_mean,
                       "preconditioner": "none (plain Lanczos)"},
         "sqrtMdotW_learned_vs_plain": cmp,
