@@ -303,3 +303,31 @@ def test_solver_selectors_check_their_arguments(lib):
         for fn, _, _, default in cases:
             fn(default)
         lib.lmg_internal_lanczos_step_shape(0, 0)
+
+
+def test_iteration_limit_and_preconditioner_rules(lib):
+    """lanczos::Solver::setIterationHardLimit's range here ([3, 250]), and the
+    learned preconditioner's host rules: kind "none" or "mlp", FP32 handles
+    only, a parameter vector of a supported network size, and no network
+    trained above a wall on an open handle.  All refused before device work."""
+    import ctypes
+    from libmobility_gb300 import precond as pc
+    s = _solver()
+    for bad in (2, 251):
+        with pytest.raises(RuntimeError, match="iteration limit"):
+            s.setLanczosIterationLimit(bad)
+    s.setLanczosIterationLimit(3)
+    s.setLanczosIterationLimit(250)
+    with pytest.raises(RuntimeError, match='"none" or "mlp"'):
+        s.setPreconditioner("bogus")
+    s.setPreconditioner("none")
+    with pytest.raises(RuntimeError, match="needs precision float"):
+        _solver(precision="double").setPreconditioner("mlp")
+    junk = np.zeros(1000, np.float32)
+    rc = s._lib.lmg_set_preconditioner(s._h, b"mlp", ctypes.c_void_p(junk.ctypes.data), junk.size)
+    assert rc != 0
+    assert "not the size of a network" in s._lib.lmg_last_error(s._h).decode()
+    wall = pc.load_weights(pc.default_weights(True), wall=True).astype(np.float32)
+    rc = s._lib.lmg_set_preconditioner(s._h, b"mlp", ctypes.c_void_p(wall.ctypes.data), wall.size)
+    assert rc != 0
+    assert "trained above a wall" in s._lib.lmg_last_error(s._h).decode()
