@@ -331,3 +331,35 @@ def test_iteration_limit_and_preconditioner_rules(lib):
     rc = s._lib.lmg_set_preconditioner(s._h, b"mlp", ctypes.c_void_p(wall.ctypes.data), wall.size)
     assert rc != 0
     assert "trained above a wall" in s._lib.lmg_last_error(s._h).decode()
+
+
+def test_noalloc_argument_rules(lib):
+    """lmg_mdot_noalloc_f32 refuses bad arguments before any device work:
+    particle count, batch size, constants, missing buffers, torques without
+    includeAngular, includeAngular without W, and host buffers (it cannot
+    stage them without allocating)."""
+    import ctypes
+    err = ctypes.create_string_buffer(256)
+    a = np.zeros((12, 3), np.float32)
+    p = ctypes.c_void_p(a.ctypes.data)
+
+    def call(pos=p, F=p, T=None, U=p, W=None, N=12, nper=-1, wall=0, eta=1.0, rad=1.0, ang=0):
+        rc = lib.lmg_mdot_noalloc_f32(pos, F, T, U, W, N, nper, wall, eta, rad, ang, None,
+                                      err, 256)
+        return rc, err.value.decode()
+
+    for kw, msg in (
+        (dict(N=0), "numberParticles must be in"),
+        (dict(N=(1 << 24) + 1), "numberParticles must be in"),
+        (dict(nper=5), "Invalid batch parameters"),
+        (dict(eta=0.0), "must be positive"),
+        (dict(rad=-1.0), "must be positive"),
+        (dict(pos=None), "needs pos, U and F and/or T"),
+        (dict(U=None), "needs pos, U and F and/or T"),
+        (dict(F=None), "needs pos, U and F and/or T"),
+        (dict(T=p), "includeAngular to true"),
+        (dict(ang=1), "needs W when includeAngular"),
+        (dict(), "device buffers only"),
+    ):
+        rc, text = call(**kw)
+        assert rc == 1 and msg in text, (kw, rc, text)
